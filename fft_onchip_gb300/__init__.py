@@ -1,0 +1,104 @@
+"""fft_onchip_gb300 — batched forward complex FFTs (N = 8..4096) on GB300.
+
+Host-side front end of libfftoc.so.  The compute path is the CUDA library;
+PyTorch only provides device memory and streams.  There is no CPU fallback:
+every call goes through the C ABI and raises FftocError if the library is
+missing or a call fails.
+
+Mirrors the per-size executor surface of gprabowski/fft_onchip
+(includes/tensor_fft_N.cuh, includes/legacy8_fft.cuh, includes/legacy16_fft.cuh):
+``tensor_fft_64(x)`` transforms every row of a (batch, 64) complex128 CUDA
+tensor, forward (exp(-2*pi*i*n*k/N)), unnormalised, natural order, like
+``fft::tensor_fft_64<CT,64>`` run by the reference harness
+(includes/testing.cuh:16-57).
+"""
+from ._lib import (ENGINE_AUTO, ENGINE_DMMA, ENGINE_F64, ENGINE_FX, ENGINES, EXPORTS, SIZES, FftocError, check,
+                   load, plan_query)
+
+__all__ = ["fft", "fft_ptr", "fft_host", "plan_query", "FftocError", "SIZES", "ENGINES", "load", "auto_engine"]
+
+
+def _engine_id(engine):
+    if isinstance(engine, str):
+        if engine not in ENGINES:
+            raise ValueError("unknown engine %r (one of %s)" % (engine, sorted(ENGINES)))
+        return ENGINES[engine]
+    return int(engine)
+
+
+def auto_engine(n):
+    return load().fftoc_auto_engine(int(n))
+
+
+def fft_ptr(n, in_ptr, out_ptr, batch, stream_ptr=0, engine="auto"):
+    """Raw C-ABI call: device pointers, batch count, cudaStream_t as int."""
+    L = load()
+    eng = _engine_id(engine)
+    if eng == ENGINE_AUTO:
+        fn = getattr(L, "fftoc_c2c_fwd_n%d" % n, None) if n in SIZES else None
+        if fn is not None:
+            return check(fn(in_ptr, out_ptr, int(batch), stream_ptr))
+        return check(L.fftoc_c2c_fwd(int(n), in_ptr, out_ptr, int(batch), stream_ptr))
+    return check(L.fftoc_c2c_fwd_ex(int(n), in_ptr, out_ptr, int(batch), eng, stream_ptr))
+
+
+def fft(x, out=None, engine="auto", stream=None):
+    """Forward FFT of every row of a (batch, n) complex128 CUDA tensor.
+
+    ``out`` may be ``x`` (in place) or a separate tensor of the same shape.
+    Runs asynchronously on ``stream`` (default: torch's current stream).
+    """
+    import torch
+
+    if not isinstance(x, torch.Tensor) or x.dtype != torch.complex128 or not x.is_cuda:
+        raise TypeError("x must be a complex128 CUDA tensor")
+    if x.dim() == 1:
+        x = x.unsqueeze(0)
+    if x.dim() != 2 or not x.is_contiguous():
+        raise ValueError("x must be a contiguous (batch, n) tensor")
+    if out is None:
+        out = torch.empty_like(x)
+    elif out.shape != x.shape or out.dtype != x.dtype or not out.is_contiguous() or out.device != x.device:
+        raise ValueError("out must match x")
+    if stream is None:
+        stream = torch.cuda.current_stream(x.device)
+    with torch.cuda.device(x.device):
+        fft_ptr(x.shape[1], x.data_ptr(), out.data_ptr(), x.shape[0], stream.cuda_stream, engine)
+    return out
+
+
+def fft_host(x_host, engine="auto", device=0):
+    """End-to-end helper: host complex128 array in, host array out (pinned
+    staging, H2D copy, transform, D2H copy, synchronise)."""
+    import numpy as np
+    import torch
+
+    a = np.ascontiguousarray(x_host, dtype=np.complex128)
+    shape = a.shape
+    a2 = a.reshape(-1, shape[-1])
+    h_in = torch.from_numpy(a2).pin_memory()
+    d = torch.empty(a2.shape, dtype=torch.complex128, device="cuda:%d" % device)
+    d.copy_(h_in, non_blocking=True)
+    fft(d, out=d, engine=engine)
+    h_out = torch.empty(a2.shape, dtype=torch.complex128, pin_memory=True)
+    h_out.copy_(d, non_blocking=True)
+    torch.cuda.synchronize(device)
+    return h_out.numpy().reshape(shape)
+
+
+def _make_size_entry(n):
+    def entry(x, out=None, engine="auto", stream=None):
+        if x.shape[-1] != n:
+            raise ValueError("tensor_fft_%d expects rows of %d points" % (n, n))
+        return fft(x, out=out, engine=engine, stream=stream)
+
+    entry.__name__ = "tensor_fft_%d" % n
+    entry.__doc__ = ("Forward %d-point FFT of every row (the reference's fft::tensor_fft_%d / legacy executor "
+                     "surface)." % (n, n))
+    return entry
+
+
+for _n in SIZES:
+    globals()["tensor_fft_%d" % _n] = _make_size_entry(_n)
+    __all__.append("tensor_fft_%d" % _n)
+del _n

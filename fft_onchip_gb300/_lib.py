@@ -1,0 +1,115 @@
+"""ctypes binding of libfftoc.so (the C ABI declared in include/fftoc.h).
+
+The library must have been built (``python -m fft_onchip_gb300.build`` or
+``__graft_entry__.build()``); there is no fallback implementation.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libfftoc.so")
+
+FFTOC_OK = 0
+STATUS_NAMES = {
+    0: "FFTOC_OK",
+    1: "FFTOC_ERR_INVALID_SIZE",
+    2: "FFTOC_ERR_INVALID_VALUE",
+    3: "FFTOC_ERR_MISALIGNED",
+    4: "FFTOC_ERR_NO_MEMORY",
+    5: "FFTOC_ERR_CUDA",
+    6: "FFTOC_ERR_TIMEOUT",
+    7: "FFTOC_ERR_UNSUPPORTED",
+}
+
+ENGINE_AUTO, ENGINE_F64, ENGINE_FX, ENGINE_DMMA = 0, 1, 2, 3
+ENGINES = {"auto": ENGINE_AUTO, "f64": ENGINE_F64, "fx": ENGINE_FX, "dmma": ENGINE_DMMA}
+
+SIZES = (8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096)
+
+# Every symbol include/fftoc.h declares.
+EXPORTS = tuple(["fftoc_c2c_fwd_n%d" % n for n in SIZES]) + (
+    "fftoc_c2c_fwd",
+    "fftoc_c2c_fwd_ex",
+    "fftoc_plan_query",
+    "fftoc_auto_engine",
+    "fftoc_status_string",
+    "fftoc_last_error_string",
+    "fftoc_version",
+)
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_int),
+        ("engine", ctypes.c_int),
+        ("threads_per_transform", ctypes.c_int),
+        ("transforms_per_block", ctypes.c_int),
+        ("threads_per_block", ctypes.c_int),
+        ("smem_bytes", ctypes.c_int),
+        ("passes", ctypes.c_int),
+        ("radix", ctypes.c_int * 4),
+    ]
+
+
+class FftocError(RuntimeError):
+    def __init__(self, status, message):
+        self.status = status
+        self.status_name = STATUS_NAMES.get(status, str(status))
+        super().__init__("%s: %s" % (self.status_name, message))
+
+
+_lib = None
+
+
+def load(path=None):
+    """Load libfftoc.so (once) and declare the C signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise FftocError(-1, "libfftoc.so not built at %s (run fft_onchip_gb300/build.py)" % path)
+    L = ctypes.CDLL(path)
+    vp, i64, c_int = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    for n in SIZES:
+        f = getattr(L, "fftoc_c2c_fwd_n%d" % n)
+        f.argtypes = [vp, vp, i64, vp]
+        f.restype = c_int
+    L.fftoc_c2c_fwd.argtypes = [c_int, vp, vp, i64, vp]
+    L.fftoc_c2c_fwd.restype = c_int
+    L.fftoc_c2c_fwd_ex.argtypes = [c_int, vp, vp, i64, c_int, vp]
+    L.fftoc_c2c_fwd_ex.restype = c_int
+    L.fftoc_plan_query.argtypes = [c_int, c_int, ctypes.POINTER(PlanInfo)]
+    L.fftoc_plan_query.restype = c_int
+    L.fftoc_auto_engine.argtypes = [c_int]
+    L.fftoc_auto_engine.restype = c_int
+    L.fftoc_status_string.argtypes = [c_int]
+    L.fftoc_status_string.restype = ctypes.c_char_p
+    L.fftoc_last_error_string.argtypes = []
+    L.fftoc_last_error_string.restype = ctypes.c_char_p
+    L.fftoc_version.argtypes = []
+    L.fftoc_version.restype = c_int
+    _lib = L
+    return L
+
+
+def check(status):
+    if status != FFTOC_OK:
+        msg = load().fftoc_last_error_string()
+        raise FftocError(status, msg.decode() if msg else "")
+    return status
+
+
+def plan_query(n, engine=ENGINE_AUTO):
+    info = PlanInfo()
+    check(load().fftoc_plan_query(int(n), int(engine), ctypes.byref(info)))
+    return {
+        "n": info.n,
+        "engine": info.engine,
+        "threads_per_transform": info.threads_per_transform,
+        "transforms_per_block": info.transforms_per_block,
+        "threads_per_block": info.threads_per_block,
+        "smem_bytes": info.smem_bytes,
+        "passes": info.passes,
+        "radix": [info.radix[i] for i in range(info.passes)],
+    }

@@ -1,0 +1,272 @@
+// fftoc — C ABI: argument checks, per-device set-up (twiddle tables, kernel
+// attributes), engine selection and launch.
+//
+// Reference behaviour replaced here: the harness of gprabowski/fft_onchip
+// (includes/testing.cuh:59-92) sets the dynamic shared-memory attribute,
+// launches fft_tester<CT,Exec,N,UPB> with grid (32*SMs)/(UPB*FPU) and block
+// (threads, UPB), and aborts the process through gpuErrchk
+// (includes/common.cuh:3-13) on any CUDA error.  This library instead returns
+// a status, keeps a per-thread message, and sizes the grid from the batch.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/fftoc.h"
+#include "fft_core.cuh"
+#include "internal.h"
+
+namespace fftoc {
+namespace {
+
+thread_local std::string t_last_error;
+
+fftoc_status fail(fftoc_status st, const std::string& msg) {
+  t_last_error = msg;
+  return st;
+}
+
+fftoc_status cuda_fail(cudaError_t e, const char* what) {
+  cudaGetLastError();  // clear a non-sticky error
+  return fail(FFTOC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// cos and sin of 2*pi*k/n in long double, with the angle reduced to
+// [0, pi/4] through the exact rational k/n (octant symmetry).
+void cos_sin(long long n, long long k, long double* c, long double* s) {
+  const long double pi = 3.141592653589793238462643383279502884L;
+  k %= n;
+  if (k < 0) k += n;
+  const long long k8 = 8 * k;
+  const long long o = k8 / n;
+  const long long r = k8 - o * n;  // angle = (pi/4) * (o + r/n)
+  long double cb, sb;
+  if (o & 1) {
+    const long double phi = (pi / 4.0L) * ((long double)(n - r) / (long double)n);
+    cb = cosl(phi);
+    sb = sinl(phi);
+    switch (((o + 1) / 2) & 3) {  // angle = q*pi/2 - phi
+      case 0: *c = cb; *s = -sb; break;
+      case 1: *c = sb; *s = cb; break;
+      case 2: *c = -cb; *s = sb; break;
+      default: *c = -sb; *s = -cb; break;
+    }
+  } else {
+    const long double phi = (pi / 4.0L) * ((long double)r / (long double)n);
+    cb = cosl(phi);
+    sb = sinl(phi);
+    switch ((o / 2) & 3) {  // angle = q*pi/2 + phi
+      case 0: *c = cb; *s = sb; break;
+      case 1: *c = -sb; *s = cb; break;
+      case 2: *c = -cb; *s = -sb; break;
+      default: *c = sb; *s = -cb; break;
+    }
+  }
+}
+
+// v * 2^61 as h*2^30 + l (0 <= l < 2^30), returned as (h, 2l)
+void fx_limbs(long double v, int* h, int* l2) {
+  const long long q = llroundl(v * 2305843009213693952.0L);  // 2^61
+  const long long hh = q >> 30;                              // arithmetic: floor
+  const long long ll = q & ((1LL << 30) - 1);
+  *h = (int)hh;
+  *l2 = (int)(2 * ll);
+}
+
+struct DeviceState {
+  std::once_flag once;
+  fftoc_status init_status = FFTOC_OK;
+  std::string init_error;
+  KernelDesc f64[kNumSizes];
+  KernelDesc fx[kNumSizes];
+  void* tw_f64[kNumSizes] = {};
+  void* tw_fx[kNumSizes] = {};
+};
+
+constexpr int kMaxDevices = 64;
+DeviceState g_devices[kMaxDevices];
+
+void build_twiddles(const KernelDesc& d, int n, std::vector<double>& f64, std::vector<int>& fx) {
+  f64.assign((size_t)d.tw_entries * 2, 0.0);
+  fx.assign((size_t)d.tw_entries * 4, 0);
+  int off = 0, p = d.radix[0];
+  for (int s = 1; s < d.passes; ++s) {
+    const int R = d.radix[s];
+    for (int m = 1; m < R; ++m)
+      for (int k = 0; k < p; ++k) {
+        long double c, sn;
+        cos_sin((long long)R * p, (long long)k * m, &c, &sn);
+        const int e = off + (m - 1) * p + k;
+        f64[2 * e] = (double)c;
+        f64[2 * e + 1] = (double)(-sn);
+        fx_limbs(c, &fx[4 * e], &fx[4 * e + 1]);
+        fx_limbs(-sn, &fx[4 * e + 2], &fx[4 * e + 3]);
+      }
+    off += (R - 1) * p;
+    p *= R;
+  }
+  (void)n;
+}
+
+void init_device(DeviceState& ds) {
+  describe_f64(ds.f64);
+  describe_fx(ds.fx);
+  for (int i = 0; i < kNumSizes; ++i) {
+    for (KernelDesc* d : {&ds.f64[i], &ds.fx[i]}) {
+      cudaError_t e = cudaFuncSetAttribute(d->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, d->smem);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        ds.init_status = FFTOC_ERR_CUDA;
+        ds.init_error = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
+        return;
+      }
+    }
+    std::vector<double> f64;
+    std::vector<int> fx;
+    build_twiddles(ds.f64[i], kSizes[i], f64, fx);
+    const size_t bytes = (size_t)(ds.f64[i].tw_entries > 0 ? ds.f64[i].tw_entries : 1) * 16;
+    for (int eng = 0; eng < 2; ++eng) {
+      void* p = nullptr;
+      cudaError_t e = cudaMalloc(&p, bytes);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        ds.init_status = FFTOC_ERR_NO_MEMORY;
+        ds.init_error = std::string("cudaMalloc(twiddles): ") + cudaGetErrorString(e);
+        return;
+      }
+      const void* src = eng == 0 ? (const void*)f64.data() : (const void*)fx.data();
+      if (ds.f64[i].tw_entries > 0) e = cudaMemcpy(p, src, (size_t)ds.f64[i].tw_entries * 16, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        ds.init_status = FFTOC_ERR_CUDA;
+        ds.init_error = std::string("cudaMemcpy(twiddles): ") + cudaGetErrorString(e);
+        return;
+      }
+      (eng == 0 ? ds.tw_f64[i] : ds.tw_fx[i]) = p;
+    }
+  }
+}
+
+fftoc_status device_state(DeviceState** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail(FFTOC_ERR_INVALID_VALUE, "device ordinal out of range");
+  DeviceState& ds = g_devices[dev];
+  std::call_once(ds.once, [&] { init_device(ds); });
+  if (ds.init_status != FFTOC_OK) return fail(ds.init_status, ds.init_error);
+  *out = &ds;
+  return FFTOC_OK;
+}
+
+int resolve_engine(int n, int engine) {
+  (void)n;
+  return engine == FFTOC_ENGINE_AUTO ? FFTOC_ENGINE_FX : engine;
+}
+
+}  // namespace
+
+fftoc_status launch_fwd(int n, const double* in, double* out, int64_t batch, int engine, cudaStream_t stream) {
+  const int idx = size_index(n);
+  if (idx < 0) return fail(FFTOC_ERR_INVALID_SIZE, "n=" + std::to_string(n) + " is not one of 8,16,...,4096");
+  if (batch < 0) return fail(FFTOC_ERR_INVALID_VALUE, "batch must be >= 0");
+  if (engine < FFTOC_ENGINE_AUTO || engine > FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_INVALID_VALUE, "unknown engine");
+  if (batch == 0) return FFTOC_OK;
+  if (!in || !out) return fail(FFTOC_ERR_INVALID_VALUE, "null buffer");
+  if (((uintptr_t)in & 15) || ((uintptr_t)out & 15)) return fail(FFTOC_ERR_MISALIGNED, "buffers must be 16-byte aligned");
+  if (batch > INT64_MAX / ((int64_t)n * 16)) return fail(FFTOC_ERR_INVALID_VALUE, "batch*n overflows");
+  const uintptr_t bytes = (uintptr_t)batch * (uintptr_t)n * 16u;
+  const uintptr_t a = (uintptr_t)in, b = (uintptr_t)out;
+  if (a != b && a < b + bytes && b < a + bytes) return fail(FFTOC_ERR_INVALID_VALUE, "in and out overlap partially");
+
+  const int eng = resolve_engine(n, engine);
+  if (eng == FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_UNSUPPORTED, "DMMA engine not available for n=" + std::to_string(n));
+  DeviceState* ds = nullptr;
+  fftoc_status st = device_state(&ds);
+  if (st != FFTOC_OK) return st;
+  const KernelDesc& d = eng == FFTOC_ENGINE_FX ? ds->fx[idx] : ds->f64[idx];
+  const void* tw = eng == FFTOC_ENGINE_FX ? ds->tw_fx[idx] : ds->tw_f64[idx];
+  const long long blocks = (batch + d.tpb - 1) / d.tpb;
+  if (blocks > 0x7FFFFFFFLL) return fail(FFTOC_ERR_INVALID_VALUE, "batch too large for one launch");
+  const double2* in2 = reinterpret_cast<const double2*>(in);
+  double2* out2 = reinterpret_cast<double2*>(out);
+  long long bl = (long long)batch;
+  void* args[] = {(void*)&in2, (void*)&out2, (void*)&bl, (void*)&tw};
+  cudaError_t e = cudaLaunchKernel(d.fn, dim3((unsigned)blocks), dim3(d.threads), args, (size_t)d.smem, stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchKernel");
+  return FFTOC_OK;
+}
+
+fftoc_status plan_query(int n, int engine, fftoc_plan_info* info) {
+  const int idx = size_index(n);
+  if (idx < 0) return fail(FFTOC_ERR_INVALID_SIZE, "n=" + std::to_string(n) + " is not one of 8,16,...,4096");
+  if (!info) return fail(FFTOC_ERR_INVALID_VALUE, "null info");
+  if (engine < FFTOC_ENGINE_AUTO || engine > FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_INVALID_VALUE, "unknown engine");
+  const int eng = resolve_engine(n, engine);
+  if (eng == FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_UNSUPPORTED, "DMMA engine not available for n=" + std::to_string(n));
+  KernelDesc d[kNumSizes];
+  if (eng == FFTOC_ENGINE_FX) describe_fx(d); else describe_f64(d);
+  info->n = n;
+  info->engine = eng;
+  info->threads_per_transform = d[idx].tpt;
+  info->transforms_per_block = d[idx].tpb;
+  info->threads_per_block = d[idx].threads;
+  info->smem_bytes = d[idx].smem;
+  info->passes = d[idx].passes;
+  for (int i = 0; i < 4; ++i) info->radix[i] = d[idx].radix[i];
+  return FFTOC_OK;
+}
+
+}  // namespace fftoc
+
+extern "C" {
+
+#define FFTOC_SIZE_ENTRY(N)                                                                       \
+  fftoc_status fftoc_c2c_fwd_n##N(const double* in, double* out, int64_t batch, fftoc_stream s) { \
+    return fftoc::launch_fwd(N, in, out, batch, FFTOC_ENGINE_AUTO, (cudaStream_t)s);            \
+  }
+FFTOC_SIZE_ENTRY(8)
+FFTOC_SIZE_ENTRY(16)
+FFTOC_SIZE_ENTRY(32)
+FFTOC_SIZE_ENTRY(64)
+FFTOC_SIZE_ENTRY(128)
+FFTOC_SIZE_ENTRY(256)
+FFTOC_SIZE_ENTRY(512)
+FFTOC_SIZE_ENTRY(1024)
+FFTOC_SIZE_ENTRY(2048)
+FFTOC_SIZE_ENTRY(4096)
+#undef FFTOC_SIZE_ENTRY
+
+fftoc_status fftoc_c2c_fwd(int n, const double* in, double* out, int64_t batch, fftoc_stream s) {
+  return fftoc::launch_fwd(n, in, out, batch, FFTOC_ENGINE_AUTO, (cudaStream_t)s);
+}
+
+fftoc_status fftoc_c2c_fwd_ex(int n, const double* in, double* out, int64_t batch, int engine, fftoc_stream s) {
+  return fftoc::launch_fwd(n, in, out, batch, engine, (cudaStream_t)s);
+}
+
+fftoc_status fftoc_plan_query(int n, int engine, fftoc_plan_info* info) { return fftoc::plan_query(n, engine, info); }
+
+int fftoc_auto_engine(int n) { return fftoc::size_index(n) < 0 ? -1 : FFTOC_ENGINE_FX; }
+
+const char* fftoc_status_string(fftoc_status s) {
+  switch (s) {
+    case FFTOC_OK: return "ok";
+    case FFTOC_ERR_INVALID_SIZE: return "invalid size";
+    case FFTOC_ERR_INVALID_VALUE: return "invalid value";
+    case FFTOC_ERR_MISALIGNED: return "misaligned buffer";
+    case FFTOC_ERR_NO_MEMORY: return "out of device memory";
+    case FFTOC_ERR_CUDA: return "CUDA error";
+    case FFTOC_ERR_TIMEOUT: return "device wait timed out";
+    case FFTOC_ERR_UNSUPPORTED: return "unsupported";
+  }
+  return "unknown status";
+}
+
+const char* fftoc_last_error_string(void) { return fftoc::t_last_error.c_str(); }
+
+int fftoc_version(void) { return FFTOC_VERSION; }
+
+}  // extern "C"

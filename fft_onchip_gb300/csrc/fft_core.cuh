@@ -1,0 +1,269 @@
+// fftoc — batched forward complex FFTs (N = 8..4096) for GB300 (sm_103a).
+//
+// Device core shared by every engine.  A transform of N points is computed by
+// T = N / P threads, each holding P points in registers.  Each pass of radix R
+// is one Stockham step (the structure of the reference's radix-8 executor,
+// includes/legacy8_fft.cuh:57-119): butterfly t' reads x[t' + m*N/R],
+// multiplies input m by W_{R*p}^{k*m} (k = t' mod p, p = product of earlier
+// radices), runs an R-point DFT and writes y[(t'-k)*R + k + m*p].  Passes are
+// joined through shared memory; the first pass reads HBM and the last writes
+// HBM, both coalesced (consecutive threads touch consecutive 16-byte points).
+//
+// Engines (arithmetic used inside the transform; input/output are always
+// interleaved binary64 complex values):
+//   EngF64 — IEEE binary64 (DFMA/DADD).
+//   EngFx  — 64-bit block fixed point.  Each transform is scaled by a power of
+//            two taken from its largest exponent so that no value can overflow
+//            (headroom for the worst-case growth of N), adds are exact 64-bit
+//            integer adds, and products use 31/30-bit limbs on IMAD.WIDE.  The
+//            conversion back to binary64 rounds once (cvt.rn.f64.s64).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fftoc {
+
+// ---------------------------------------------------------------------------
+// Plans: points per thread P and the radix of each pass (product = N).
+// ---------------------------------------------------------------------------
+template <int N> struct Plan;
+template <> struct Plan<8>    { static constexpr int P = 8,  S = 1; static constexpr int R[4] = {8, 1, 1, 1}; };
+template <> struct Plan<16>   { static constexpr int P = 16, S = 1; static constexpr int R[4] = {16, 1, 1, 1}; };
+template <> struct Plan<32>   { static constexpr int P = 8,  S = 2; static constexpr int R[4] = {8, 4, 1, 1}; };
+template <> struct Plan<64>   { static constexpr int P = 8,  S = 2; static constexpr int R[4] = {8, 8, 1, 1}; };
+template <> struct Plan<128>  { static constexpr int P = 16, S = 2; static constexpr int R[4] = {16, 8, 1, 1}; };
+template <> struct Plan<256>  { static constexpr int P = 16, S = 2; static constexpr int R[4] = {16, 16, 1, 1}; };
+template <> struct Plan<512>  { static constexpr int P = 8,  S = 3; static constexpr int R[4] = {8, 8, 8, 1}; };
+template <> struct Plan<1024> { static constexpr int P = 16, S = 3; static constexpr int R[4] = {16, 8, 8, 1}; };
+template <> struct Plan<2048> { static constexpr int P = 16, S = 3; static constexpr int R[4] = {16, 16, 8, 1}; };
+template <> struct Plan<4096> { static constexpr int P = 8,  S = 4; static constexpr int R[4] = {8, 8, 8, 8}; };
+
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
+
+// span p of pass s (product of the radices before it)
+template <int N> __host__ __device__ constexpr int span_of(int s) {
+  int p = 1;
+  for (int i = 0; i < s; ++i) p *= Plan<N>::R[i];
+  return p;
+}
+// offset (in twiddle entries) of pass s's table; pass s holds (R-1)*p entries,
+// entry (m-1)*p + k = W_{R p}^{k m}.  Pass 0 has no twiddles.
+template <int N> __host__ __device__ constexpr int tw_offset(int s) {
+  int off = 0;
+  for (int i = 1; i < s; ++i) off += (Plan<N>::R[i] - 1) * span_of<N>(i);
+  return off;
+}
+template <int N> __host__ __device__ constexpr int tw_count() { return tw_offset<N>(Plan<N>::S); }
+
+// ---------------------------------------------------------------------------
+// Engines
+// ---------------------------------------------------------------------------
+struct EngF64 {
+  using S = double;
+  using TW = double2;   // (cos, -sin) of the twiddle
+  struct KC { double c; };
+  static constexpr int kId = 1;
+  __device__ __forceinline__ static S add(S a, S b) { return a + b; }
+  __device__ __forceinline__ static S sub(S a, S b) { return a - b; }
+  __device__ __forceinline__ static S mulc(S x, KC k) { return x * k.c; }
+  __device__ __forceinline__ static void cmul(S& xr, S& xi, const TW w) {
+    const double r = fma(xr, w.x, -xi * w.y);
+    const double i = fma(xr, w.y, xi * w.x);
+    xr = r;
+    xi = i;
+  }
+  // complex multiply by a compile-time constant (c, s)
+  __device__ __forceinline__ static void cmulk(S& xr, S& xi, KC c, KC s) {
+    const double r = fma(xr, c.c, -xi * s.c);
+    const double i = fma(xr, s.c, xi * c.c);
+    xr = r;
+    xi = i;
+  }
+};
+
+struct EngFx {
+  using S = long long;
+  using TW = int4;      // (wr.h, wr.l2, wi.h, wi.l2): w*2^61 = h*2^30 + l, l2 = 2l
+  struct KC { int h, l2; };
+  static constexpr int kId = 2;
+  __device__ __forceinline__ static S add(S a, S b) { return a + b; }
+  __device__ __forceinline__ static S sub(S a, S b) { return a - b; }
+  // x * c for a real constant c, |x| < 2^61.  With x = xh*2^31 + xl:
+  //   x*c = xh*ch + (xh*cl2 + xl*ch) / 2^31 + xl*cl/2^61 (last term < 1, dropped)
+  __device__ __forceinline__ static S mulc(S x, KC k) {
+    const int xh = (int)(x >> 31);
+    const int xl = (int)((unsigned)x & 0x7FFFFFFFu);
+    const long long m = (long long)xh * k.l2 + (long long)xl * k.h + (1LL << 30);
+    return (long long)xh * k.h + (m >> 31);
+  }
+  __device__ __forceinline__ static void cmul(S& xr, S& xi, const TW w) {
+    const int rh = (int)(xr >> 31), rl = (int)((unsigned)xr & 0x7FFFFFFFu);
+    const int ih = (int)(xi >> 31), il = (int)((unsigned)xi & 0x7FFFFFFFu);
+    const long long mr = (long long)rh * w.y + (long long)rl * w.x + (long long)(-ih) * w.w +
+                         (long long)(-il) * w.z + (1LL << 30);
+    const long long mi = (long long)rh * w.w + (long long)rl * w.z + (long long)ih * w.y +
+                         (long long)il * w.x + (1LL << 30);
+    xr = (long long)rh * w.x + (long long)(-ih) * w.z + (mr >> 31);
+    xi = (long long)rh * w.z + (long long)ih * w.x + (mi >> 31);
+  }
+  __device__ __forceinline__ static void cmulk(S& xr, S& xi, KC c, KC s) {
+    const int4 w = make_int4(c.h, c.l2, s.h, s.l2);
+    cmul(xr, xi, w);
+  }
+};
+
+// constants of the DFT kernels, per engine
+template <class E> struct Konst;
+template <> struct Konst<EngF64> {
+  // sqrt(1/2), cos(pi/8), sin(pi/8)
+  __device__ __forceinline__ static EngF64::KC h() { return {0.70710678118654752440}; }
+  __device__ __forceinline__ static EngF64::KC nh() { return {-0.70710678118654752440}; }
+  __device__ __forceinline__ static EngF64::KC c8() { return {0.92387953251128675613}; }
+  __device__ __forceinline__ static EngF64::KC s8() { return {0.38268343236508977173}; }
+  __device__ __forceinline__ static EngF64::KC nc8() { return {-0.92387953251128675613}; }
+  __device__ __forceinline__ static EngF64::KC ns8() { return {-0.38268343236508977173}; }
+};
+// Q2.61 fixed-point limbs of the same constants: v*2^61 = h*2^30 + l, l2 = 2l.
+template <> struct Konst<EngFx> {
+  __device__ __forceinline__ static EngFx::KC h() { return {1518500249, 2121767202}; }
+  __device__ __forceinline__ static EngFx::KC nh() { return {-1518500250, 25716446}; }
+  __device__ __forceinline__ static EngFx::KC c8() { return {1984016188, 1696238674}; }
+  __device__ __forceinline__ static EngFx::KC s8() { return {821806413, 782852818}; }
+  __device__ __forceinline__ static EngFx::KC nc8() { return {-1984016189, 451244974}; }
+  __device__ __forceinline__ static EngFx::KC ns8() { return {-821806414, 1364630830}; }
+};
+
+// ---------------------------------------------------------------------------
+// Small forward DFTs on registers.  re[i], im[i] at compile-time indices
+// base + stride*m, in place, natural order.
+// ---------------------------------------------------------------------------
+template <class E, int B, int ST, int PP>
+__device__ __forceinline__ void dft2(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
+  using S = typename E::S;
+  const S ar = re[B], ai = im[B], br = re[B + ST], bi = im[B + ST];
+  re[B] = E::add(ar, br); im[B] = E::add(ai, bi);
+  re[B + ST] = E::sub(ar, br); im[B + ST] = E::sub(ai, bi);
+}
+
+template <class E, int B, int ST, int PP>
+__device__ __forceinline__ void dft4(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
+  using S = typename E::S;
+  const S s0r = E::add(re[B], re[B + 2 * ST]), s0i = E::add(im[B], im[B + 2 * ST]);
+  const S d0r = E::sub(re[B], re[B + 2 * ST]), d0i = E::sub(im[B], im[B + 2 * ST]);
+  const S s1r = E::add(re[B + ST], re[B + 3 * ST]), s1i = E::add(im[B + ST], im[B + 3 * ST]);
+  const S d1r = E::sub(re[B + ST], re[B + 3 * ST]), d1i = E::sub(im[B + ST], im[B + 3 * ST]);
+  re[B] = E::add(s0r, s1r); im[B] = E::add(s0i, s1i);
+  re[B + 2 * ST] = E::sub(s0r, s1r); im[B + 2 * ST] = E::sub(s0i, s1i);
+  // y1 = d0 - i*d1, y3 = d0 + i*d1
+  re[B + ST] = E::add(d0r, d1i); im[B + ST] = E::sub(d0i, d1r);
+  re[B + 3 * ST] = E::sub(d0r, d1i); im[B + 3 * ST] = E::add(d0i, d1r);
+}
+
+// 8-point DFT: radix-2 split into two 4-point DFTs; W8^1, W8^3 as real
+// constant products (sqrt(1/2)).
+template <class E, int B, int ST, int PP>
+__device__ __forceinline__ void dft8(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
+  using S = typename E::S;
+  using K = Konst<E>;
+  S ar[4], ai[4], br[4], bi[4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    ar[m] = E::add(re[B + m * ST], re[B + (m + 4) * ST]);
+    ai[m] = E::add(im[B + m * ST], im[B + (m + 4) * ST]);
+    br[m] = E::sub(re[B + m * ST], re[B + (m + 4) * ST]);
+    bi[m] = E::sub(im[B + m * ST], im[B + (m + 4) * ST]);
+  }
+  // b1 *= (1 - i)/sqrt2 ; b2 *= -i ; b3 *= (-1 - i)/sqrt2
+  {
+    const S r = E::mulc(E::add(br[1], bi[1]), K::h());
+    const S i = E::mulc(E::sub(bi[1], br[1]), K::h());
+    br[1] = r; bi[1] = i;
+    const S r2 = bi[2], i2 = br[2];  // (-i)*(x+iy) = y - i x : im becomes -br[2]
+    br[2] = r2; bi[2] = i2;           // bi[2] holds +br[2]; sign folded below
+    const S r3 = E::mulc(E::sub(bi[3], br[3]), K::h());
+    const S i3 = E::mulc(E::add(br[3], bi[3]), K::nh());
+    br[3] = r3; bi[3] = i3;
+  }
+  // even outputs: DFT4(a)
+  {
+    const S s0r = E::add(ar[0], ar[2]), s0i = E::add(ai[0], ai[2]);
+    const S d0r = E::sub(ar[0], ar[2]), d0i = E::sub(ai[0], ai[2]);
+    const S s1r = E::add(ar[1], ar[3]), s1i = E::add(ai[1], ai[3]);
+    const S d1r = E::sub(ar[1], ar[3]), d1i = E::sub(ai[1], ai[3]);
+    re[B] = E::add(s0r, s1r); im[B] = E::add(s0i, s1i);
+    re[B + 4 * ST] = E::sub(s0r, s1r); im[B + 4 * ST] = E::sub(s0i, s1i);
+    re[B + 2 * ST] = E::add(d0r, d1i); im[B + 2 * ST] = E::sub(d0i, d1r);
+    re[B + 6 * ST] = E::sub(d0r, d1i); im[B + 6 * ST] = E::add(d0i, d1r);
+  }
+  // odd outputs: DFT4(b0, b1', b2', b3'), with b2' = (bi2, -br2) stored as (br[2], bi[2]) = (bi2, br2)
+  {
+    // b2' real = br[2], b2' imag = -bi[2]
+    const S s0r = E::add(br[0], br[2]), s0i = E::sub(bi[0], bi[2]);
+    const S d0r = E::sub(br[0], br[2]), d0i = E::add(bi[0], bi[2]);
+    const S s1r = E::add(br[1], br[3]), s1i = E::add(bi[1], bi[3]);
+    const S d1r = E::sub(br[1], br[3]), d1i = E::sub(bi[1], bi[3]);
+    re[B + ST] = E::add(s0r, s1r); im[B + ST] = E::add(s0i, s1i);
+    re[B + 5 * ST] = E::sub(s0r, s1r); im[B + 5 * ST] = E::sub(s0i, s1i);
+    re[B + 3 * ST] = E::add(d0r, d1i); im[B + 3 * ST] = E::sub(d0i, d1r);
+    re[B + 7 * ST] = E::sub(d0r, d1i); im[B + 7 * ST] = E::add(d0i, d1r);
+  }
+}
+
+// 16-point DFT: two 8-point DFTs (even / odd samples) and a radix-2 combine
+// with W16^k.
+template <class E, int B, int ST, int PP>
+__device__ __forceinline__ void dft16(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
+  using S = typename E::S;
+  using K = Konst<E>;
+  // even samples at B + 2m*ST, odd at B + (2m+1)*ST
+  dft8<E, B, 2 * ST, PP>(re, im);
+  dft8<E, B + ST, 2 * ST, PP>(re, im);
+  // O[k] *= W16^k, k = 1..7
+  {
+    S r, i;
+    // k=1: (c8, -s8)
+    r = re[B + 3 * ST]; i = im[B + 3 * ST]; E::cmulk(r, i, K::c8(), K::ns8()); re[B + 3 * ST] = r; im[B + 3 * ST] = i;
+    // k=2: (1-i)/sqrt2
+    r = re[B + 5 * ST]; i = im[B + 5 * ST];
+    re[B + 5 * ST] = E::mulc(E::add(r, i), K::h()); im[B + 5 * ST] = E::mulc(E::sub(i, r), K::h());
+    // k=3: (s8, -c8)
+    r = re[B + 7 * ST]; i = im[B + 7 * ST]; E::cmulk(r, i, K::s8(), K::nc8()); re[B + 7 * ST] = r; im[B + 7 * ST] = i;
+    // k=4: -i
+    r = re[B + 9 * ST]; i = im[B + 9 * ST]; re[B + 9 * ST] = i; im[B + 9 * ST] = E::sub(S(0), r);
+    // k=5: (-s8, -c8)
+    r = re[B + 11 * ST]; i = im[B + 11 * ST]; E::cmulk(r, i, K::ns8(), K::nc8()); re[B + 11 * ST] = r; im[B + 11 * ST] = i;
+    // k=6: (-1-i)/sqrt2
+    r = re[B + 13 * ST]; i = im[B + 13 * ST];
+    re[B + 13 * ST] = E::mulc(E::sub(i, r), K::h()); im[B + 13 * ST] = E::mulc(E::add(r, i), K::nh());
+    // k=7: (-c8, -s8)
+    r = re[B + 15 * ST]; i = im[B + 15 * ST]; E::cmulk(r, i, K::nc8(), K::ns8()); re[B + 15 * ST] = r; im[B + 15 * ST] = i;
+  }
+  // combine: X[k] = E[k] + O[k], X[k+8] = E[k] - O[k]; E[k] at B + 2k*ST, O[k] at B + (2k+1)*ST
+  S xr[16], xi[16];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const S er = re[B + 2 * k * ST], ei = im[B + 2 * k * ST];
+    const S orr = re[B + (2 * k + 1) * ST], oi = im[B + (2 * k + 1) * ST];
+    xr[k] = E::add(er, orr); xi[k] = E::add(ei, oi);
+    xr[k + 8] = E::sub(er, orr); xi[k + 8] = E::sub(ei, oi);
+  }
+#pragma unroll
+  for (int k = 0; k < 16; ++k) { re[B + k * ST] = xr[k]; im[B + k * ST] = xi[k]; }
+}
+
+template <class E, int R, int B, int ST, int PP>
+__device__ __forceinline__ void dft(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
+  if constexpr (R == 2) dft2<E, B, ST, PP>(re, im);
+  else if constexpr (R == 4) dft4<E, B, ST, PP>(re, im);
+  else if constexpr (R == 8) dft8<E, B, ST, PP>(re, im);
+  else if constexpr (R == 16) dft16<E, B, ST, PP>(re, im);
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory layout: element e of a transform lives at 16-byte slot
+// e ^ ((e >> SW) & 7).  Writes of the first pass go at stride R (=2^SW) points
+// per thread; the XOR keeps 8 consecutive threads on 8 distinct bank groups.
+// ---------------------------------------------------------------------------
+template <int SW> __device__ __forceinline__ int swz(int e) { return e ^ ((e >> SW) & 7); }
+
+}  // namespace fftoc

@@ -1,0 +1,265 @@
+// fftoc — the batched forward-FFT kernel template (one launch = `batch`
+// transforms of size N, TPB transforms per CTA).
+#pragma once
+#include <utility>
+#include "fft_core.cuh"
+
+namespace fftoc {
+
+// Fixed-point scale: input magnitudes are mapped below 2^FxBits<N>, leaving
+// log2(N) + 2 bits of headroom under 2^63 (worst-case growth N, plus the
+// sqrt(2)-scaled sums inside the radix-8/16 kernels and the 2^61 limit of the
+// limb products).
+template <int N> struct FxBits {
+  static constexpr int B = (61 - ilog2c(N)) < 53 ? (61 - ilog2c(N)) : 53;
+};
+
+// --- binary64 <-> block fixed point -------------------------------------------
+__device__ __forceinline__ int expo_of(unsigned hw) { return (int)((hw >> 20) & 0x7FFu); }
+
+// value * 2^(1022 + B - Emax) truncated toward zero; eref = Emax + 53 - B.
+__device__ __forceinline__ long long fx_in(unsigned hw, unsigned lw, int eref) {
+  const int e = expo_of(hw);
+  const unsigned mh = (hw & 0xFFFFFu) | (e ? 0x100000u : 0u);
+  const int d = min(eref - max(e, 1), 63);
+  const unsigned long long m = ((((unsigned long long)mh) << 32) | lw) >> d;
+  const long long r = (long long)m;
+  return ((int)hw < 0) ? -r : r;
+}
+
+// x * 2^K, K = Emax - 1022 - B.  Fast path adds K to the exponent field of the
+// correctly rounded conversion (exact); `slow` transforms (result exponents
+// outside the normal range) use ldexp.
+__device__ __forceinline__ double fx_out(long long x, int kshift, int K, bool slow) {
+  const double d = (double)x;
+  if (slow) return ldexp(d, K);
+  const int hi = __double2hiint(d);
+  const int lo = __double2loint(d);
+  return __hiloint2double(x != 0 ? hi + kshift : hi, lo);
+}
+
+// --- the kernel ---------------------------------------------------------------
+template <class E, int N, int TPB>
+struct Fft {
+  using S = typename E::S;
+  using TW = typename E::TW;
+  static constexpr int P = Plan<N>::P;
+  static constexpr int T = N / P;
+  static constexpr int NS = Plan<N>::S;
+  static constexpr int SW = ilog2c(Plan<N>::R[0]);
+  static constexpr int THREADS = T * TPB;
+  static constexpr bool STAGED = T < 8;  // small N: stage HBM tiles through smem
+  static constexpr int SMEM = TPB * N * 16 + 64;
+
+  // 16-byte slot of element e of block-local transform j
+  __device__ __forceinline__ static int slot(int j, int e) {
+    return j * N + (e ^ (((e >> SW) ^ (j * T)) & 7));
+  }
+
+  template <int s, int b>
+  __device__ __forceinline__ static void butterfly(S (&re)[P], S (&im)[P], int t, const TW* __restrict__ tw) {
+    constexpr int R = Plan<N>::R[s];
+    constexpr int B = P / R;
+    constexpr int p = span_of<N>(s);
+    if constexpr (s > 0) {
+      const int tp = t + T * b;
+      const int k = tp & (p - 1);
+      const TW* base = tw + tw_offset<N>(s) + k;
+#pragma unroll
+      for (int m = 1; m < R; ++m) {
+        const TW w = __ldg(base + (m - 1) * p);
+        E::cmul(re[b + B * m], im[b + B * m], w);
+      }
+    }
+    dft<E, R, b, B, P>(re, im);
+  }
+
+  template <int s, int... bs>
+  __device__ __forceinline__ static void pass(S (&re)[P], S (&im)[P], int t, const TW* __restrict__ tw,
+                                              std::integer_sequence<int, bs...>) {
+    (butterfly<s, bs>(re, im, t, tw), ...);
+  }
+
+  // destination index of output m of butterfly b in pass s
+  template <int s>
+  __device__ __forceinline__ static int dest(int t, int b, int m) {
+    constexpr int R = Plan<N>::R[s];
+    constexpr int p = span_of<N>(s);
+    const int tp = t + T * b;
+    const int k = tp & (p - 1);
+    return (tp - k) * R + k + m * p;
+  }
+
+  template <int s>
+  __device__ __forceinline__ static void write_smem(S (&re)[P], S (&im)[P], int j, int t, longlong2* sm) {
+    constexpr int R = Plan<N>::R[s];
+    constexpr int B = P / R;
+#pragma unroll
+    for (int b = 0; b < B; ++b)
+#pragma unroll
+      for (int m = 0; m < R; ++m) {
+        longlong2 v;
+        v.x = to_bits(re[b + B * m]);
+        v.y = to_bits(im[b + B * m]);
+        sm[slot(j, dest<s>(t, b, m))] = v;
+      }
+  }
+
+  __device__ __forceinline__ static void read_smem(S (&re)[P], S (&im)[P], int j, int t, const longlong2* sm) {
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      const longlong2 v = sm[slot(j, t + T * i)];
+      re[i] = from_bits(v.x);
+      im[i] = from_bits(v.y);
+    }
+  }
+  __device__ __forceinline__ static long long to_bits(S v) {
+    if constexpr (E::kId == EngF64::kId) return __double_as_longlong(v);
+    else return (long long)v;
+  }
+  __device__ __forceinline__ static S from_bits(long long b) {
+    if constexpr (E::kId == EngF64::kId) return __longlong_as_double(b);
+    else return (S)b;
+  }
+
+  template <int s>
+  __device__ __forceinline__ static void run_passes(S (&re)[P], S (&im)[P], int j, int t, const TW* __restrict__ tw,
+                                                    longlong2* sm) {
+    constexpr int R = Plan<N>::R[s];
+    pass<s>(re, im, t, tw, std::make_integer_sequence<int, P / R>{});
+    if constexpr (s + 1 < NS) {
+      if constexpr (s > 0) __syncthreads();  // previous readers of the buffer are done
+      write_smem<s>(re, im, j, t, sm);
+      __syncthreads();
+      read_smem(re, im, j, t, sm);
+      run_passes<s + 1>(re, im, j, t, tw, sm);
+    }
+  }
+};
+
+// Engine-specific entry/exit: load raw points (binary64), convert, run the
+// passes, convert back and store.
+template <class E, int N, int TPB>
+__global__ void __launch_bounds__(Fft<E, N, TPB>::THREADS)
+fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long long batch,
+               const typename E::TW* __restrict__ tw) {
+  using F = Fft<E, N, TPB>;
+  using S = typename E::S;
+  constexpr int P = F::P, T = F::T, NS = F::NS;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  longlong2* sm = reinterpret_cast<longlong2*>(smem_raw);
+
+  const int tid = threadIdx.x;
+  const int j = tid / T;
+  const int t = tid - j * T;
+  const long long tile0 = (long long)blockIdx.x * TPB;
+  const long long tr = tile0 + j;
+  const bool active = tr < batch;
+  const long long tile_elems = (min((long long)TPB, batch - tile0)) * N;
+
+  // ---- load raw binary64 points: point i of this thread is element t + T*i
+  double2 raw[P];
+  if constexpr (F::STAGED) {
+    const double2* src = in + tile0 * N;
+    for (int idx = tid; idx < tile_elems; idx += F::THREADS) {
+      const int jj = idx / N, e = idx - jj * N;
+      const double2 v = __ldg(src + idx);
+      sm[F::slot(jj, e)] = make_longlong2(__double_as_longlong(v.x), __double_as_longlong(v.y));
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      const longlong2 v = sm[F::slot(j, t + T * i)];
+      raw[i] = make_double2(__longlong_as_double(v.x), __longlong_as_double(v.y));
+    }
+  } else {
+    const double2* src = in + tr * N + t;
+#pragma unroll
+    for (int i = 0; i < P; ++i) raw[i] = active ? __ldg(src + T * i) : make_double2(0.0, 0.0);
+  }
+
+  S re[P], im[P];
+  int K = 0, kshift = 0;
+  bool slow = false, special = false;
+  if constexpr (E::kId == EngF64::kId) {
+#pragma unroll
+    for (int i = 0; i < P; ++i) { re[i] = raw[i].x; im[i] = raw[i].y; }
+  } else {
+    // largest biased exponent of the transform
+    int em = 0;
+#pragma unroll
+    for (int i = 0; i < P; ++i)
+      em = max(em, max(expo_of(__double2hiint(raw[i].x)), expo_of(__double2hiint(raw[i].y))));
+    if constexpr (T > 1 && T <= 32) {
+#pragma unroll
+      for (int o = T / 2; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o, T));
+    } else if constexpr (T > 32) {
+      // warps of one transform are contiguous: reduce per warp, then in smem
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
+      int* red = reinterpret_cast<int*>(smem_raw + TPB * N * 16);
+      if (tid < TPB) red[tid] = 0;
+      __syncthreads();
+      if ((tid & 31) == 0) atomicMax(&red[j], em);
+      __syncthreads();
+      em = red[j];
+    }
+    constexpr int B = FxBits<N>::B;
+    special = (em == 0x7FF);
+    K = em - 1022 - B;
+    kshift = K << 20;
+    slow = (em < B) || (em > 1983 + B);
+    const int eref = em + 53 - B;
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      re[i] = fx_in((unsigned)__double2hiint(raw[i].x), (unsigned)__double2loint(raw[i].x), eref);
+      im[i] = fx_in((unsigned)__double2hiint(raw[i].y), (unsigned)__double2loint(raw[i].y), eref);
+    }
+  }
+
+  if constexpr (F::STAGED) __syncthreads();  // staging buffer is reused by the passes
+  F::template run_passes<0>(re, im, j, t, tw, sm);
+
+  // ---- store: output m of butterfly b of the last pass is element dest(...)
+  constexpr int RL = Plan<N>::R[NS - 1];
+  constexpr int BL = P / RL;
+  auto result = [&](int i) -> double2 {
+    if constexpr (E::kId == EngF64::kId) {
+      return make_double2(re[i], im[i]);
+    } else {
+      if (special) {
+        const double qnan = __longlong_as_double(0x7FF8000000000000LL);
+        return make_double2(qnan, qnan);
+      }
+      return make_double2(fx_out((long long)re[i], kshift, K, slow), fx_out((long long)im[i], kshift, K, slow));
+    }
+  };
+  if constexpr (F::STAGED) {
+    if constexpr (NS > 1) __syncthreads();
+#pragma unroll
+    for (int b = 0; b < BL; ++b)
+#pragma unroll
+      for (int m = 0; m < RL; ++m) {
+        const double2 v = result(b + BL * m);
+        sm[F::slot(j, F::template dest<NS - 1>(t, b, m))] =
+            make_longlong2(__double_as_longlong(v.x), __double_as_longlong(v.y));
+      }
+    __syncthreads();
+    double2* dst = out + tile0 * N;
+    for (int idx = tid; idx < tile_elems; idx += F::THREADS) {
+      const int jj = idx / N, e = idx - jj * N;
+      const longlong2 v = sm[F::slot(jj, e)];
+      dst[idx] = make_double2(__longlong_as_double(v.x), __longlong_as_double(v.y));
+    }
+  } else {
+    if (active) {
+      double2* dst = out + tr * N;
+#pragma unroll
+      for (int b = 0; b < BL; ++b)
+#pragma unroll
+        for (int m = 0; m < RL; ++m) dst[F::template dest<NS - 1>(t, b, m)] = result(b + BL * m);
+    }
+  }
+}
+
+}  // namespace fftoc

@@ -1,0 +1,121 @@
+/*
+ * fftoc — batched forward complex FFTs of N = 8..4096 points on one GB300.
+ *
+ * C ABI of the library (libfftoc.so).  It replaces the per-size executor
+ * surface of gprabowski/fft_onchip, where every size N has its own device
+ * executor type driven by the test harness:
+ *   includes/tensor_fft_8.cuh:12-66      tensor_fft_8<CT,8,UPB,FPU>
+ *   includes/tensor_fft_16.cuh:9-63      tensor_fft_16 (does not compile upstream)
+ *   includes/tensor_fft_64.cuh:12-77     tensor_fft_64
+ *   includes/tensor_fft_128.cuh:12-101   tensor_fft_128
+ *   includes/tensor_fft_256.cuh:10-123   tensor_fft_256
+ *   includes/tensor_fft_512.cuh:12-122   tensor_fft_512
+ *   includes/tensor_fft_4096.cuh:12-98   tensor_fft_4096
+ *   includes/legacy8_fft.cuh:11-120      legacy_fft<CT,N>     (N a power of 8)
+ *   includes/legacy16_fft.cuh:17-173     legacy16_fft<CT,N>   (N a power of 16)
+ * and the harness entry that stages data and launches them,
+ *   includes/testing.cuh:16-57 (fft_tester), :59-92 (run_fft_kernel).
+ * There, one launch transforms a contiguous batch of N-point transforms of
+ * thrust::complex<double> (includes/config.hpp:6), in place, forward
+ * (exp(-2*pi*i*n*k/N)), unnormalised, natural order.  The reference has no
+ * sizes 32, 1024 or 2048; they are provided here with the same contract.
+ *
+ * Conventions of every transform entry point:
+ *   - in/out are DEVICE pointers to batch*n interleaved (re, im) doubles,
+ *     16-byte aligned; transform b occupies doubles [2*n*b, 2*n*(b+1)).
+ *   - in == out (in place) is allowed; other overlaps are rejected.
+ *   - calls are asynchronous on `stream` (0 = legacy default stream); they
+ *     never call exit() and never synchronise.
+ *   - errors are returned as fftoc_status; fftoc_last_error_string() gives a
+ *     per-thread message for the last failing call.
+ *   - the library owns its twiddle tables (built on the host in long double,
+ *     uploaded once per device on first use); the caller owns the buffers.
+ *   - thread safe across host threads.
+ *   - results agree with the exact DFT to relative L2 error <= 1e-13 for
+ *     every engine of the FP64 form (see fftoc_engine).
+ */
+#ifndef FFTOC_H
+#define FFTOC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FFTOC_VERSION 10000 /* 1.0.0 */
+
+typedef enum {
+  FFTOC_OK = 0,
+  FFTOC_ERR_INVALID_SIZE = 1,  /* n is not one of 8,16,...,4096            */
+  FFTOC_ERR_INVALID_VALUE = 2, /* null pointer, negative batch, bad enum,
+                                  partial overlap, batch too large          */
+  FFTOC_ERR_MISALIGNED = 3,    /* buffer not 16-byte aligned               */
+  FFTOC_ERR_NO_MEMORY = 4,     /* device allocation failed                 */
+  FFTOC_ERR_CUDA = 5,          /* CUDA runtime error                       */
+  FFTOC_ERR_TIMEOUT = 6,       /* a bounded device wait gave up            */
+  FFTOC_ERR_UNSUPPORTED = 7    /* engine not available for this n         */
+} fftoc_status;
+
+/* Arithmetic used inside a transform (input/output are always binary64). */
+typedef enum {
+  FFTOC_ENGINE_AUTO = 0, /* fastest engine of the FP64 form for this n           */
+  FFTOC_ENGINE_F64 = 1,  /* IEEE binary64 (DFMA/DADD)                            */
+  FFTOC_ENGINE_FX = 2,   /* 64-bit block fixed point: per-transform power-of-two
+                            scale, exact integer adds, 62-bit twiddles;
+                            relative L2 error ~1e-15                             */
+  FFTOC_ENGINE_DMMA = 3  /* Karatsuba complex GEMM on FP64 mma.m8n8k4
+                            (the reference's tensor_utils.cuh:32-36 scheme)      */
+} fftoc_engine;
+
+typedef struct CUstream_st *fftoc_stream; /* same type as cudaStream_t */
+
+/* One entry per size (reference: the tensor_fft_N / legacy executors above). */
+fftoc_status fftoc_c2c_fwd_n8(const double *in, double *out, int64_t batch, fftoc_stream stream);
+fftoc_status fftoc_c2c_fwd_n16(const double *in, double *out, int64_t batch, fftoc_stream stream);
+fftoc_status fftoc_c2c_fwd_n32(const double *in, double *out, int64_t batch, fftoc_stream stream);
+fftoc_status fftoc_c2c_fwd_n64(const double *in, double *out, int64_t batch, fftoc_stream stream);
+fftoc_status fftoc_c2c_fwd_n128(const double *in, double *out, int64_t batch, fftoc_stream stream);
+fftoc_status fftoc_c2c_fwd_n256(const double *in, double *out, int64_t batch, fftoc_stream stream);
+fftoc_status fftoc_c2c_fwd_n512(const double *in, double *out, int64_t batch, fftoc_stream stream);
+fftoc_status fftoc_c2c_fwd_n1024(const double *in, double *out, int64_t batch, fftoc_stream stream);
+fftoc_status fftoc_c2c_fwd_n2048(const double *in, double *out, int64_t batch, fftoc_stream stream);
+fftoc_status fftoc_c2c_fwd_n4096(const double *in, double *out, int64_t batch, fftoc_stream stream);
+
+/* Size as a runtime argument (reference: run_fft_kernel<CT,Size,FFTExec>,
+ * includes/testing.cuh:59-92, with Size a template argument). */
+fftoc_status fftoc_c2c_fwd(int n, const double *in, double *out, int64_t batch, fftoc_stream stream);
+
+/* Same, with an explicit engine. */
+fftoc_status fftoc_c2c_fwd_ex(int n, const double *in, double *out, int64_t batch, int engine,
+                              fftoc_stream stream);
+
+/* Launch geometry of a size/engine (reference: the FFTExec static members
+ * threads / units_per_block / ffts_per_unit, e.g. tensor_fft_64.cuh:16-19). */
+typedef struct {
+  int n;
+  int engine;                 /* resolved engine (never AUTO)               */
+  int threads_per_transform;  /* lanes cooperating on one transform         */
+  int transforms_per_block;   /* transforms per CTA                          */
+  int threads_per_block;
+  int smem_bytes;             /* dynamic shared memory per CTA               */
+  int passes;                 /* Stockham passes                             */
+  int radix[4];               /* radix of each pass                          */
+} fftoc_plan_info;
+
+fftoc_status fftoc_plan_query(int n, int engine, fftoc_plan_info *info);
+
+/* Engine that FFTOC_ENGINE_AUTO resolves to for size n. */
+int fftoc_auto_engine(int n);
+
+/* Messages. */
+const char *fftoc_status_string(fftoc_status status);
+const char *fftoc_last_error_string(void);
+int fftoc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FFTOC_H */

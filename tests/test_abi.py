@@ -1,0 +1,94 @@
+"""CPU tests of the C ABI: the library loads, exports every symbol that
+include/fftoc.h declares, and rejects bad arguments before touching a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from fft_onchip_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    syms = set()
+    for name in os.listdir(os.path.join(ROOT, "include")):
+        if name.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", name)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            syms |= set(re.findall(r"\b(fftoc_\w+)\s*\(", text))
+    return syms
+
+
+def test_header_declares_the_size_surface():
+    syms = declared_symbols()
+    for n in _lib.SIZES:
+        assert "fftoc_c2c_fwd_n%d" % n in syms
+    assert {"fftoc_c2c_fwd", "fftoc_c2c_fwd_ex", "fftoc_last_error_string"} <= syms
+
+
+def test_library_exports_every_declared_symbol(fftoc_lib):
+    missing = [s for s in sorted(declared_symbols()) if not hasattr(fftoc_lib, s)]
+    assert not missing, missing
+    assert set(_lib.EXPORTS) <= declared_symbols()
+
+
+def test_version_and_status_strings(fftoc_lib):
+    assert fftoc_lib.fftoc_version() >= 10000
+    for st in range(8):
+        assert fftoc_lib.fftoc_status_string(st)
+
+
+@pytest.mark.parametrize("n", _lib.SIZES)
+@pytest.mark.parametrize("engine", ["auto", "f64", "fx"])
+def test_plan_query(fftoc_lib, n, engine):
+    p = _lib.plan_query(n, _lib.ENGINES[engine])
+    assert p["n"] == n
+    assert p["engine"] in (_lib.ENGINE_F64, _lib.ENGINE_FX)
+    prod = 1
+    for r in p["radix"]:
+        prod *= r
+    assert prod == n
+    assert p["threads_per_transform"] * p["transforms_per_block"] == p["threads_per_block"]
+    assert p["threads_per_block"] <= 1024 and p["smem_bytes"] <= 227 * 1024
+
+
+def _call(L, n, inp, out, batch, engine=0):
+    return L.fftoc_c2c_fwd_ex(n, inp, out, batch, engine, None)
+
+
+def test_argument_errors_without_gpu(fftoc_lib):
+    L = fftoc_lib
+    A = 1 << 20  # aligned fake device addresses: never dereferenced on these paths
+    assert _call(L, 48, A, A, 4) == 1                     # FFTOC_ERR_INVALID_SIZE
+    assert b"48" in L.fftoc_last_error_string()
+    assert L.fftoc_c2c_fwd(100, A, A, 4, None) == 1
+    assert _call(L, 64, A, A, -1) == 2                    # negative batch
+    assert _call(L, 64, A, A, 0) == 0                     # empty batch: no-op
+    assert _call(L, 64, None, A, 4) == 2                  # null
+    assert _call(L, 64, A + 8, A + 8, 4) == 3             # misaligned
+    assert _call(L, 64, A, A + 16, 4) == 2                # partial overlap
+    assert _call(L, 64, A, A, 4, engine=9) == 2           # unknown engine
+    assert _call(L, 64, A, A, 1 << 62) == 2               # batch*n overflows
+    assert L.fftoc_auto_engine(64) in (_lib.ENGINE_F64, _lib.ENGINE_FX)
+    assert L.fftoc_auto_engine(65) == -1
+
+
+def test_python_front_end_raises(fftoc_lib):
+    import fft_onchip_gb300 as F
+    with pytest.raises(F.FftocError) as ei:
+        F.fft_ptr(48, 1 << 20, 1 << 20, 4)
+    assert ei.value.status == 1
+    with pytest.raises(ValueError):
+        F.fft_ptr(64, 1 << 20, 1 << 20, 4, engine="nope")
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    with pytest.raises(_lib.FftocError):
+        saved = _lib._lib
+        _lib._lib = None
+        try:
+            _lib.load(str(tmp_path / "libfftoc.so"))
+        finally:
+            _lib._lib = saved
