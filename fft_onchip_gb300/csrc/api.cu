@@ -66,13 +66,11 @@ void cos_sin(long long n, long long k, long double* c, long double* s) {
   }
 }
 
-// v * 2^61 as h*2^30 + l (0 <= l < 2^30), returned as (h, 2l)
-void fx_limbs(long double v, int* h, int* l2) {
-  const long long q = llroundl(v * 2305843009213693952.0L);  // 2^61
-  const long long hh = q >> 30;                              // arithmetic: floor
-  const long long ll = q & ((1LL << 30) - 1);
-  *h = (int)hh;
-  *l2 = (int)(2 * ll);
+// v * 2^60 as h*2^30 + l with 0 <= l < 2^30 (|v| <= 1 gives |h| <= 2^30)
+void fx_limbs(long double v, int* h, int* l) {
+  const long long q = llroundl(v * 1152921504606846976.0L);  // 2^60
+  *h = (int)(q >> 30);                                       // arithmetic: floor
+  *l = (int)(q & ((1LL << 30) - 1));
 }
 
 struct DeviceState {

@@ -15,11 +15,13 @@
 //   EngFx  — 64-bit block fixed point.  Each transform is scaled by a power of
 //            two taken from its largest exponent so that no value can overflow
 //            (headroom for the worst-case growth of N), adds are exact 64-bit
-//            integer adds, and products use 31/30-bit limbs on IMAD.WIDE.  The
+//            integer adds, and products use 30-bit limbs on IMAD.WIDE.  The
 //            conversion back to binary64 rounds once (cvt.rn.f64.s64).
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+
+#define FFTOC_HD __host__ __device__ __forceinline__
 
 namespace fftoc {
 
@@ -63,17 +65,17 @@ struct EngF64 {
   using TW = double2;   // (cos, -sin) of the twiddle
   struct KC { double c; };
   static constexpr int kId = 1;
-  __device__ __forceinline__ static S add(S a, S b) { return a + b; }
-  __device__ __forceinline__ static S sub(S a, S b) { return a - b; }
-  __device__ __forceinline__ static S mulc(S x, KC k) { return x * k.c; }
-  __device__ __forceinline__ static void cmul(S& xr, S& xi, const TW w) {
+  FFTOC_HD static S add(S a, S b) { return a + b; }
+  FFTOC_HD static S sub(S a, S b) { return a - b; }
+  FFTOC_HD static S mulc(S x, KC k) { return x * k.c; }
+  FFTOC_HD static void cmul(S& xr, S& xi, const TW w) {
     const double r = fma(xr, w.x, -xi * w.y);
     const double i = fma(xr, w.y, xi * w.x);
     xr = r;
     xi = i;
   }
   // complex multiply by a compile-time constant (c, s)
-  __device__ __forceinline__ static void cmulk(S& xr, S& xi, KC c, KC s) {
+  FFTOC_HD static void cmulk(S& xr, S& xi, KC c, KC s) {
     const double r = fma(xr, c.c, -xi * s.c);
     const double i = fma(xr, s.c, xi * c.c);
     xr = r;
@@ -83,54 +85,61 @@ struct EngF64 {
 
 struct EngFx {
   using S = long long;
-  using TW = int4;      // (wr.h, wr.l2, wi.h, wi.l2): w*2^61 = h*2^30 + l, l2 = 2l
-  struct KC { int h, l2; };
+  using TW = int4;      // (wr.h, wr.l, wi.h, wi.l): w*2^60 = h*2^30 + l, 0 <= l < 2^30
+  struct KC { int h, l; };
   static constexpr int kId = 2;
-  __device__ __forceinline__ static S add(S a, S b) { return a + b; }
-  __device__ __forceinline__ static S sub(S a, S b) { return a - b; }
-  // x * c for a real constant c, |x| < 2^61.  With x = xh*2^31 + xl:
-  //   x*c = xh*ch + (xh*cl2 + xl*ch) / 2^31 + xl*cl/2^61 (last term < 1, dropped)
-  __device__ __forceinline__ static S mulc(S x, KC k) {
-    const int xh = (int)(x >> 31);
-    const int xl = (int)((unsigned)x & 0x7FFFFFFFu);
-    const long long m = (long long)xh * k.l2 + (long long)xl * k.h + (1LL << 30);
-    return (long long)xh * k.h + (m >> 31);
+  FFTOC_HD static S add(S a, S b) { return a + b; }
+  FFTOC_HD static S sub(S a, S b) { return a - b; }
+  // Limbs of a value, |x| < 2^61: x = xh*2^30 + xl, |xh| < 2^31, 0 <= xl < 2^30.
+  FFTOC_HD static void split(S x, int& xh, int& xl) {
+    xh = (int)(x >> 30);
+    xl = (int)((unsigned)x & 0x3FFFFFFFu);
   }
-  __device__ __forceinline__ static void cmul(S& xr, S& xi, const TW w) {
-    const int rh = (int)(xr >> 31), rl = (int)((unsigned)xr & 0x7FFFFFFFu);
-    const int ih = (int)(xi >> 31), il = (int)((unsigned)xi & 0x7FFFFFFFu);
-    const long long mr = (long long)rh * w.y + (long long)rl * w.x + (long long)(-ih) * w.w +
-                         (long long)(-il) * w.z + (1LL << 30);
-    const long long mi = (long long)rh * w.w + (long long)rl * w.z + (long long)ih * w.y +
-                         (long long)il * w.x + (1LL << 30);
-    xr = (long long)rh * w.x + (long long)(-ih) * w.z + (mr >> 31);
-    xi = (long long)rh * w.z + (long long)ih * w.x + (mi >> 31);
+  // x * c for a real constant, |c| <= 1:
+  //   x*c = xh*ch + (xh*cl + xl*ch) / 2^30 + xl*cl/2^60   (last term < 1, dropped)
+  // |xh*cl| < 2^61, |xl*ch| <= 2^60, so the middle sum cannot overflow.
+  FFTOC_HD static S mulc(S x, KC k) {
+    int xh, xl;
+    split(x, xh, xl);
+    const long long m = (long long)xh * k.l + (long long)xl * k.h + (1LL << 29);
+    return (long long)xh * k.h + (m >> 30);
   }
-  __device__ __forceinline__ static void cmulk(S& xr, S& xi, KC c, KC s) {
-    const int4 w = make_int4(c.h, c.l2, s.h, s.l2);
-    cmul(xr, xi, w);
+  // (xr + i xi) * (wr + i wi); each middle sum has four terms of magnitude
+  // < 2^61 or <= 2^60, so |m| < 1.5 * 2^62.
+  FFTOC_HD static void cmul_limbs(S& xr, S& xi, int wrh, int wrl, int wih, int wil) {
+    int rh, rl, ih, il;
+    split(xr, rh, rl);
+    split(xi, ih, il);
+    const long long mr = (long long)rh * wrl + (long long)rl * wrh - (long long)ih * wil - (long long)il * wih +
+                         (1LL << 29);
+    const long long mi = (long long)rh * wil + (long long)rl * wih + (long long)ih * wrl + (long long)il * wrh +
+                         (1LL << 29);
+    xr = (long long)rh * wrh - (long long)ih * wih + (mr >> 30);
+    xi = (long long)rh * wih + (long long)ih * wrh + (mi >> 30);
   }
+  FFTOC_HD static void cmul(S& xr, S& xi, const int4 w) { cmul_limbs(xr, xi, w.x, w.y, w.z, w.w); }
+  FFTOC_HD static void cmulk(S& xr, S& xi, KC c, KC s) { cmul_limbs(xr, xi, c.h, c.l, s.h, s.l); }
 };
 
 // constants of the DFT kernels, per engine
 template <class E> struct Konst;
 template <> struct Konst<EngF64> {
   // sqrt(1/2), cos(pi/8), sin(pi/8)
-  __device__ __forceinline__ static EngF64::KC h() { return {0.70710678118654752440}; }
-  __device__ __forceinline__ static EngF64::KC nh() { return {-0.70710678118654752440}; }
-  __device__ __forceinline__ static EngF64::KC c8() { return {0.92387953251128675613}; }
-  __device__ __forceinline__ static EngF64::KC s8() { return {0.38268343236508977173}; }
-  __device__ __forceinline__ static EngF64::KC nc8() { return {-0.92387953251128675613}; }
-  __device__ __forceinline__ static EngF64::KC ns8() { return {-0.38268343236508977173}; }
+  FFTOC_HD static EngF64::KC h() { return {0.70710678118654752440}; }
+  FFTOC_HD static EngF64::KC nh() { return {-0.70710678118654752440}; }
+  FFTOC_HD static EngF64::KC c8() { return {0.92387953251128675613}; }
+  FFTOC_HD static EngF64::KC s8() { return {0.38268343236508977173}; }
+  FFTOC_HD static EngF64::KC nc8() { return {-0.92387953251128675613}; }
+  FFTOC_HD static EngF64::KC ns8() { return {-0.38268343236508977173}; }
 };
-// Q2.61 fixed-point limbs of the same constants: v*2^61 = h*2^30 + l, l2 = 2l.
+// Fixed-point limbs of the same constants: v*2^60 = h*2^30 + l, 0 <= l < 2^30.
 template <> struct Konst<EngFx> {
-  __device__ __forceinline__ static EngFx::KC h() { return {1518500249, 2121767202}; }
-  __device__ __forceinline__ static EngFx::KC nh() { return {-1518500250, 25716446}; }
-  __device__ __forceinline__ static EngFx::KC c8() { return {1984016188, 1696238674}; }
-  __device__ __forceinline__ static EngFx::KC s8() { return {821806413, 782852818}; }
-  __device__ __forceinline__ static EngFx::KC nc8() { return {-1984016189, 451244974}; }
-  __device__ __forceinline__ static EngFx::KC ns8() { return {-821806414, 1364630830}; }
+  FFTOC_HD static EngFx::KC h() { return {759250124, 1067312712}; }
+  FFTOC_HD static EngFx::KC nh() { return {-759250125, 6429112}; }
+  FFTOC_HD static EngFx::KC c8() { return {992008094, 424059668}; }
+  FFTOC_HD static EngFx::KC s8() { return {410903206, 732584116}; }
+  FFTOC_HD static EngFx::KC nc8() { return {-992008095, 649682156}; }
+  FFTOC_HD static EngFx::KC ns8() { return {-410903207, 341157708}; }
 };
 
 // ---------------------------------------------------------------------------
@@ -138,7 +147,7 @@ template <> struct Konst<EngFx> {
 // base + stride*m, in place, natural order.
 // ---------------------------------------------------------------------------
 template <class E, int B, int ST, int PP>
-__device__ __forceinline__ void dft2(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
+FFTOC_HD void dft2(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
   using S = typename E::S;
   const S ar = re[B], ai = im[B], br = re[B + ST], bi = im[B + ST];
   re[B] = E::add(ar, br); im[B] = E::add(ai, bi);
@@ -146,7 +155,7 @@ __device__ __forceinline__ void dft2(typename E::S (&re)[PP], typename E::S (&im
 }
 
 template <class E, int B, int ST, int PP>
-__device__ __forceinline__ void dft4(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
+FFTOC_HD void dft4(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
   using S = typename E::S;
   const S s0r = E::add(re[B], re[B + 2 * ST]), s0i = E::add(im[B], im[B + 2 * ST]);
   const S d0r = E::sub(re[B], re[B + 2 * ST]), d0i = E::sub(im[B], im[B + 2 * ST]);
@@ -162,7 +171,7 @@ __device__ __forceinline__ void dft4(typename E::S (&re)[PP], typename E::S (&im
 // 8-point DFT: radix-2 split into two 4-point DFTs; W8^1, W8^3 as real
 // constant products (sqrt(1/2)).
 template <class E, int B, int ST, int PP>
-__device__ __forceinline__ void dft8(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
+FFTOC_HD void dft8(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
   using S = typename E::S;
   using K = Konst<E>;
   S ar[4], ai[4], br[4], bi[4];
@@ -212,7 +221,7 @@ __device__ __forceinline__ void dft8(typename E::S (&re)[PP], typename E::S (&im
 // 16-point DFT: two 8-point DFTs (even / odd samples) and a radix-2 combine
 // with W16^k.
 template <class E, int B, int ST, int PP>
-__device__ __forceinline__ void dft16(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
+FFTOC_HD void dft16(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
   using S = typename E::S;
   using K = Konst<E>;
   // even samples at B + 2m*ST, odd at B + (2m+1)*ST
@@ -252,7 +261,7 @@ __device__ __forceinline__ void dft16(typename E::S (&re)[PP], typename E::S (&i
 }
 
 template <class E, int R, int B, int ST, int PP>
-__device__ __forceinline__ void dft(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
+FFTOC_HD void dft(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
   if constexpr (R == 2) dft2<E, B, ST, PP>(re, im);
   else if constexpr (R == 4) dft4<E, B, ST, PP>(re, im);
   else if constexpr (R == 8) dft8<E, B, ST, PP>(re, im);
@@ -264,6 +273,6 @@ __device__ __forceinline__ void dft(typename E::S (&re)[PP], typename E::S (&im)
 // e ^ ((e >> SW) & 7).  Writes of the first pass go at stride R (=2^SW) points
 // per thread; the XOR keeps 8 consecutive threads on 8 distinct bank groups.
 // ---------------------------------------------------------------------------
-template <int SW> __device__ __forceinline__ int swz(int e) { return e ^ ((e >> SW) & 7); }
+template <int SW> FFTOC_HD int swz(int e) { return e ^ ((e >> SW) & 7); }
 
 }  // namespace fftoc

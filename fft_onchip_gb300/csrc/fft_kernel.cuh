@@ -1,6 +1,7 @@
 // fftoc — the batched forward-FFT kernel template (one launch = `batch`
 // transforms of size N, TPB transforms per CTA).
 #pragma once
+#include <cstring>
 #include <utility>
 #include "fft_core.cuh"
 
@@ -15,13 +16,44 @@ template <int N> struct FxBits {
 };
 
 // --- binary64 <-> block fixed point -------------------------------------------
-__device__ __forceinline__ int expo_of(unsigned hw) { return (int)((hw >> 20) & 0x7FFu); }
+FFTOC_HD unsigned hi_word(double v) {
+#ifdef __CUDA_ARCH__
+  return (unsigned)__double2hiint(v);
+#else
+  unsigned long long b;
+  memcpy(&b, &v, 8);
+  return (unsigned)(b >> 32);
+#endif
+}
+FFTOC_HD unsigned lo_word(double v) {
+#ifdef __CUDA_ARCH__
+  return (unsigned)__double2loint(v);
+#else
+  unsigned long long b;
+  memcpy(&b, &v, 8);
+  return (unsigned)b;
+#endif
+}
+FFTOC_HD double from_words(unsigned hi, unsigned lo) {
+#ifdef __CUDA_ARCH__
+  return __hiloint2double((int)hi, (int)lo);
+#else
+  const unsigned long long b = ((unsigned long long)hi << 32) | lo;
+  double v;
+  memcpy(&v, &b, 8);
+  return v;
+#endif
+}
+
+FFTOC_HD int expo_of(unsigned hw) { return (int)((hw >> 20) & 0x7FFu); }
 
 // value * 2^(1022 + B - Emax) truncated toward zero; eref = Emax + 53 - B.
-__device__ __forceinline__ long long fx_in(unsigned hw, unsigned lw, int eref) {
+FFTOC_HD long long fx_in(unsigned hw, unsigned lw, int eref) {
   const int e = expo_of(hw);
   const unsigned mh = (hw & 0xFFFFFu) | (e ? 0x100000u : 0u);
-  const int d = min(eref - max(e, 1), 63);
+  const int ee = e > 1 ? e : 1;
+  const int d0 = eref - ee;
+  const int d = d0 < 63 ? d0 : 63;
   const unsigned long long m = ((((unsigned long long)mh) << 32) | lw) >> d;
   const long long r = (long long)m;
   return ((int)hw < 0) ? -r : r;
@@ -30,12 +62,27 @@ __device__ __forceinline__ long long fx_in(unsigned hw, unsigned lw, int eref) {
 // x * 2^K, K = Emax - 1022 - B.  Fast path adds K to the exponent field of the
 // correctly rounded conversion (exact); `slow` transforms (result exponents
 // outside the normal range) use ldexp.
-__device__ __forceinline__ double fx_out(long long x, int kshift, int K, bool slow) {
+FFTOC_HD double fx_out(long long x, int kshift, int K, bool slow) {
   const double d = (double)x;
   if (slow) return ldexp(d, K);
-  const int hi = __double2hiint(d);
-  const int lo = __double2loint(d);
-  return __hiloint2double(x != 0 ? hi + kshift : hi, lo);
+  const unsigned hi = hi_word(d);
+  return from_words(x != 0 ? hi + (unsigned)kshift : hi, lo_word(d));
+}
+
+// Scale parameters of a transform from its largest biased exponent.
+struct FxScale {
+  int eref, K, kshift;
+  bool slow, special;
+};
+template <int B>
+FFTOC_HD FxScale fx_scale(int em) {
+  FxScale s;
+  s.special = (em == 0x7FF);
+  s.K = em - 1022 - B;
+  s.kshift = (int)((unsigned)s.K << 20);
+  s.slow = (em < B) || (em > 1983 + B);
+  s.eref = em + 53 - B;
+  return s;
 }
 
 // --- the kernel ---------------------------------------------------------------
@@ -189,7 +236,7 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
     int em = 0;
 #pragma unroll
     for (int i = 0; i < P; ++i)
-      em = max(em, max(expo_of(__double2hiint(raw[i].x)), expo_of(__double2hiint(raw[i].y))));
+      em = max(em, max(expo_of(hi_word(raw[i].x)), expo_of(hi_word(raw[i].y))));
     if constexpr (T > 1 && T <= 32) {
 #pragma unroll
       for (int o = T / 2; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o, T));
@@ -204,16 +251,16 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
       __syncthreads();
       em = red[j];
     }
-    constexpr int B = FxBits<N>::B;
-    special = (em == 0x7FF);
-    K = em - 1022 - B;
-    kshift = K << 20;
-    slow = (em < B) || (em > 1983 + B);
-    const int eref = em + 53 - B;
+    const FxScale sc = fx_scale<FxBits<N>::B>(em);
+    special = sc.special;
+    K = sc.K;
+    kshift = sc.kshift;
+    slow = sc.slow;
+    const int eref = sc.eref;
 #pragma unroll
     for (int i = 0; i < P; ++i) {
-      re[i] = fx_in((unsigned)__double2hiint(raw[i].x), (unsigned)__double2loint(raw[i].x), eref);
-      im[i] = fx_in((unsigned)__double2hiint(raw[i].y), (unsigned)__double2loint(raw[i].y), eref);
+      re[i] = fx_in(hi_word(raw[i].x), lo_word(raw[i].x), eref);
+      im[i] = fx_in(hi_word(raw[i].y), lo_word(raw[i].y), eref);
     }
   }
 

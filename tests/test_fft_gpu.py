@@ -32,8 +32,11 @@ def run(torch, x, engine="auto", inplace=False):
 
 
 def per_transform_err(a, b):
-    num = np.linalg.norm(a - b, axis=1)
-    den = np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+    # rows rescaled by their largest |b| first, so 1e300-sized values do not overflow
+    s = np.max(np.abs(b), axis=1, keepdims=True)
+    s[s == 0] = 1.0
+    num = np.linalg.norm((a - b) / s, axis=1)
+    den = np.maximum(np.linalg.norm(b / s, axis=1), 1e-300)
     return num / den
 
 
