@@ -1,0 +1,372 @@
+"""Benchmark: batched forward complex-FP64 FFTs on GB300 through the C ABI.
+
+Workload (one "step"): the plain-FP64 size sweep — N in {8, 16, 64, 128, 256,
+512, 4096}, each a batch of 1 GiB of complex128 input (so 2 GiB of HBM
+traffic per size), one call of the library's per-size entry point each.
+Inputs are N(0,1) re/im from a seeded device generator, resident in HBM
+before timing; every buffer is larger than L2 (129 MB), so no L2 flush is
+needed between steps.
+
+Prints ONE JSON line (rank 0).  `value` = FFTs/s over the whole sweep
+(total transforms / total time, max over ranks); per-size FFT/s and % of the
+measured HBM copy bandwidth are in `per_n`.  `e2e` repeats the sweep through
+fftoc_c2c_fwd_host with pinned host buffers (host->device copy, transform,
+device->host copy inside the timed region).
+
+--impl reference times the CPU restatement of the path (the reference has no
+CPU implementation; oracle/fftoc_oracle.c's FP64 Stockham port of its
+radix-8 executor) on all host cores, one bounded sample per size per step.
+
+Multi-GPU: torchrun --nproc-per-node N; each rank runs the full sweep on its
+own GPU (independent transforms, no collective on the data path: weak
+scaling); barrier + max over ranks around the timed region.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SWEEP = (8, 16, 64, 128, 256, 512, 4096)
+GIB = 1 << 30
+METRIC = "FFTs/s, %HBM peak: split vs FP64 at err<=1e-11; serve p50/p99"
+WORKLOAD = "plain FP64 size sweep: N in {8,16,64,128,256,512,4096}, 1 GiB complex128 input per N"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--engine", default="auto")
+    ap.add_argument("--sizes", default=",".join(str(n) for n in SWEEP))
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=1.5, help="CPU-baseline sample time per size")
+    ap.add_argument("--gib", type=float, default=1.0, help="input GiB per size (1.0 = the sweep configuration)")
+    return ap.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_table():
+    """Per-launch DRAM bytes from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if _cuda_ok() else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def _cuda_ok():
+    import torch
+    return torch.cuda.is_available()
+
+
+def allreduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], device="cuda" if _cuda_ok() else "cpu", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ----------------------------------------------------------------------------
+# CPU baseline: the oracle's FP64 Stockham port on all host cores
+# ----------------------------------------------------------------------------
+def cpu_sample_rate(sizes, seconds_per_size):
+    from fft_onchip_gb300 import inputs
+    from oracle import oracle as O
+    threads = O.max_threads()
+    total_ffts, total_t, per = 0, 0.0, {}
+    for n in sizes:
+        batch = (GIB // (16 * n))
+        sample = max(1, batch // 64)
+        x = inputs.normal(n, sample, seed=n)
+        O.fft_f64(x[: max(1, sample // 16)], threads=0)  # warm the pool and caches
+        t0 = time.perf_counter()
+        reps = 0
+        while True:
+            O.fft_f64(x, threads=0)
+            reps += 1
+            el = time.perf_counter() - t0
+            if el >= seconds_per_size:
+                break
+        total_ffts += reps * sample
+        total_t += el
+        per[str(n)] = reps * sample / el
+    return total_ffts / total_t, threads, per
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    sizes = [int(s) for s in args.sizes.split(",")]
+    from oracle import oracle as O
+    from fft_onchip_gb300 import inputs
+    threads = O.max_threads()
+    samples = {}
+    for n in sizes:
+        batch = GIB // (16 * n)
+        samples[n] = inputs.normal(n, max(1, batch // 32), seed=n)
+    for _ in range(args.warmup):
+        for n in sizes:
+            O.fft_f64(samples[n], threads=0)
+    t0 = time.perf_counter()
+    ffts = 0
+    for _ in range(args.steps):
+        for n in sizes:
+            O.fft_f64(samples[n], threads=0)
+            ffts += samples[n].shape[0]
+    el = time.perf_counter() - t0
+    value = ffts / el
+    desc = "1/32 of each size's 1 GiB batch per step (%s transforms)" % (
+        "+".join(str(samples[n].shape[0]) for n in sizes))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "FFT/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": desc, "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": "FFT/s", "cores": threads, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": value, "unit": "FFT/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------
+def run_ours(args, world, rank, local):
+    import torch
+    import fft_onchip_gb300 as F
+    from oracle import oracle as O
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = F.load()
+    sizes = [int(s) for s in args.sizes.split(",")]
+    eng = F._engine_id(args.engine)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    bufs = {}
+    for n in sizes:
+        batch = int(args.gib * GIB) // (16 * n)
+        g = torch.Generator(device=dev).manual_seed(1000 * rank + n)
+        x = torch.randn(batch, n, dtype=torch.complex128, device=dev, generator=g)
+        y = torch.empty_like(x)
+        bufs[n] = (x, y, batch)
+    torch.cuda.synchronize()
+
+    def launch(n):
+        x, y, batch = bufs[n]
+        if eng == F.ENGINE_AUTO:
+            F.check(getattr(L, "fftoc_c2c_fwd_n%d" % n)(x.data_ptr(), y.data_ptr(), batch, sptr))
+        else:
+            F.check(L.fftoc_c2c_fwd_ex(n, x.data_ptr(), y.data_ptr(), batch, eng, sptr))
+
+    for _ in range(max(3, args.warmup)):
+        for n in sizes:
+            launch(n)
+    torch.cuda.synchronize()
+
+    K = args.steps
+    ev = {n: [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+          for n in sizes}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler.start()
+    time.sleep(0.3)
+    e0.record(stream)
+    for k in range(K):
+        for n in sizes:
+            ev[n][k][0].record(stream)
+            launch(n)
+            ev[n][k][1].record(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = sampler.stop()
+    t_ms = allreduce_max(e0.elapsed_time(e1), world)
+
+    total_ffts = world * K * sum(bufs[n][2] for n in sizes)
+    value = total_ffts / (t_ms * 1e-3)
+    hbm, peak_kind = peaks()
+    per_n, launch_ms = {}, {}
+    for n in sizes:
+        ms = [a.elapsed_time(b) for a, b in ev[n]]
+        avg = float(np.mean(ms))
+        launch_ms[n] = avg
+        batch = bufs[n][2]
+        gbs = 32.0 * n * batch / (avg * 1e-3) / 1e9
+        per_n[str(n)] = {"batch": batch, "ms": round(avg, 4), "fft_per_s": batch / (avg * 1e-3),
+                         "hbm_gbs": round(gbs, 1), "frac_hbm": round(gbs / hbm, 4)}
+    dom = max(sizes, key=lambda n: launch_ms[n])
+    dom_gbs = 32.0 * dom * bufs[dom][2] / (launch_ms[dom] * 1e-3) / 1e9
+    tt = traffic_table()
+    traffic = tt.get(str(dom), {}).get(F.plan_query(dom, eng)["engine"] == F.ENGINE_FX and "fx" or "f64")
+    roofline = {"bound": "hbm", "achieved": round(dom_gbs, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(dom_gbs / hbm, 4), "traffic": traffic,
+                "kernel": "fft_fwd_kernel N=%d (%s)" % (dom, "fx" if F.plan_query(dom, eng)["engine"] == F.ENGINE_FX else "f64"),
+                "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured" else "fallback 6800 GB/s",
+                "algorithmic_bytes_per_launch": 32 * dom * bufs[dom][2]}
+
+    # correctness guard on the timed outputs: 64 transforms per size vs the oracle
+    max_err = 0.0
+    for n in sizes:
+        x, y, batch = bufs[n]
+        idx = torch.arange(0, batch, max(1, batch // 64), device=dev)[:64]
+        ref = O.fft_f64(x[idx].cpu().numpy())
+        max_err = max(max_err, O.rel_l2(y[idx].cpu().numpy(), ref))
+
+    # end to end through fftoc_c2c_fwd_host, pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        hb = max(bufs[n][2] * n for n in sizes)
+        h_in = torch.empty(hb, dtype=torch.complex128, pin_memory=True)
+        h_out = torch.empty(hb, dtype=torch.complex128, pin_memory=True)
+        h_in.copy_(bufs[sizes[0]][0].reshape(-1)[:hb].cpu())
+        for n in sizes:  # warm-up (allocates staging once)
+            F.check(L.fftoc_c2c_fwd_host(n, h_in.data_ptr(), h_out.data_ptr(), bufs[n][2], eng, sptr))
+        torch.cuda.synchronize()
+        E = max(1, args.e2e_steps)
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(E):
+            for n in sizes:
+                F.check(L.fftoc_c2c_fwd_host(n, h_in.data_ptr(), h_out.data_ptr(), bufs[n][2], eng, sptr))
+            stream.synchronize()
+        el = allreduce_max(time.perf_counter() - t0, world)
+        bytes_step = sum(bufs[n][2] * n * 16 for n in sizes)
+        e2e = {"value": world * E * sum(bufs[n][2] for n in sizes) / el, "unit": "FFT/s",
+               "h2d_bytes_per_step": bytes_step, "d2h_bytes_per_step": bytes_step,
+               "steps": E, "ms_per_step": 1e3 * el / E, "path": "fftoc_c2c_fwd_host (pinned, 64 MiB chunks)"}
+        del h_in, h_out
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, cores, per = cpu_sample_rate(sizes, args.cpu_seconds)
+        cpu = {"value": v, "unit": "FFT/s", "cores": cores, "kind": "port",
+               "sample": "oracle FP64 Stockham (radix-8/4/2) on 1/64 of each size's batch, >= %.1f s per size"
+                         % args.cpu_seconds, "per_n": {k: round(val, 1) for k, val in per.items()}}
+
+    if rank == 0:
+        resolved = sorted({F.plan_query(n, eng)["engine"] for n in sizes})
+        dtype = "int64 block fixed point (complex128 in/out)" if resolved == [F.ENGINE_FX] else (
+            "f64" if resolved == [F.ENGINE_F64] else "mixed f64/int64")
+        line = {
+            "metric": METRIC, "value": value, "unit": "FFT/s", "n_gpus": world, "steps": K,
+            "warmup": max(3, args.warmup), "ms_per_step": t_ms / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sizes": sizes, "engine": args.engine,
+                       "bytes_per_step": sum(32 * n * bufs[n][2] for n in sizes),
+                       "l2": "inputs and outputs (1 GiB each per size) larger than L2; no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "per_n": per_n, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": K * len(sizes), "clocks": clocks, "max_rel_err_vs_oracle": max_err,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -15,7 +15,7 @@ tensor, forward (exp(-2*pi*i*n*k/N)), unnormalised, natural order, like
 from ._lib import (ENGINE_AUTO, ENGINE_DMMA, ENGINE_F64, ENGINE_FX, ENGINES, EXPORTS, SIZES, FftocError, check,
                    load, plan_query)
 
-__all__ = ["fft", "fft_ptr", "fft_host", "plan_query", "FftocError", "SIZES", "ENGINES", "load", "auto_engine"]
+__all__ = ["fft", "fft_ptr", "fft_host", "fft_host_ptr", "plan_query", "FftocError", "SIZES", "ENGINES", "load", "auto_engine"]
 
 
 def _engine_id(engine):
@@ -67,23 +67,30 @@ def fft(x, out=None, engine="auto", stream=None):
     return out
 
 
-def fft_host(x_host, engine="auto", device=0):
-    """End-to-end helper: host complex128 array in, host array out (pinned
-    staging, H2D copy, transform, D2H copy, synchronise)."""
+def fft_host_ptr(n, h_in_ptr, h_out_ptr, batch, stream_ptr=0, engine="auto"):
+    """Raw C-ABI call on HOST pointers (fftoc_c2c_fwd_host)."""
+    return check(load().fftoc_c2c_fwd_host(int(n), h_in_ptr, h_out_ptr, int(batch), _engine_id(engine), stream_ptr))
+
+
+def fft_host(x_host, out=None, engine="auto", device=0):
+    """End-to-end call with host memory: a numpy complex128 (batch, n) array
+    (or a pinned CPU torch tensor) in, same out.  Blocks until done."""
     import numpy as np
     import torch
 
-    a = np.ascontiguousarray(x_host, dtype=np.complex128)
-    shape = a.shape
-    a2 = a.reshape(-1, shape[-1])
-    h_in = torch.from_numpy(a2).pin_memory()
-    d = torch.empty(a2.shape, dtype=torch.complex128, device="cuda:%d" % device)
-    d.copy_(h_in, non_blocking=True)
-    fft(d, out=d, engine=engine)
-    h_out = torch.empty(a2.shape, dtype=torch.complex128, pin_memory=True)
-    h_out.copy_(d, non_blocking=True)
-    torch.cuda.synchronize(device)
-    return h_out.numpy().reshape(shape)
+    if isinstance(x_host, torch.Tensor):
+        src = x_host
+    else:
+        src = torch.from_numpy(np.ascontiguousarray(x_host, dtype=np.complex128))
+    if src.dim() == 1:
+        src = src.unsqueeze(0)
+    if out is None:
+        out = torch.empty_like(src)
+    with torch.cuda.device(device):
+        stream = torch.cuda.current_stream()
+        fft_host_ptr(src.shape[-1], src.data_ptr(), out.data_ptr(), src.shape[0], stream.cuda_stream, engine)
+        stream.synchronize()
+    return out.numpy() if not isinstance(x_host, torch.Tensor) else out
 
 
 def _make_size_entry(n):

@@ -30,6 +30,7 @@ SIZES = (8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096)
 EXPORTS = tuple(["fftoc_c2c_fwd_n%d" % n for n in SIZES]) + (
     "fftoc_c2c_fwd",
     "fftoc_c2c_fwd_ex",
+    "fftoc_c2c_fwd_host",
     "fftoc_plan_query",
     "fftoc_auto_engine",
     "fftoc_status_string",
@@ -79,6 +80,8 @@ def load(path=None):
     L.fftoc_c2c_fwd.restype = c_int
     L.fftoc_c2c_fwd_ex.argtypes = [c_int, vp, vp, i64, c_int, vp]
     L.fftoc_c2c_fwd_ex.restype = c_int
+    L.fftoc_c2c_fwd_host.argtypes = [c_int, vp, vp, i64, c_int, vp]
+    L.fftoc_c2c_fwd_host.restype = c_int
     L.fftoc_plan_query.argtypes = [c_int, c_int, ctypes.POINTER(PlanInfo)]
     L.fftoc_plan_query.restype = c_int
     L.fftoc_auto_engine.argtypes = [c_int]

@@ -73,7 +73,23 @@ void fx_limbs(long double v, int* h, int* l) {
   *l = (int)(q & ((1LL << 30) - 1));
 }
 
+// Device staging for host-buffer calls: three chunk buffers cycled through
+// H2D -> transform -> D2H on three streams.
+struct Staging {
+  static constexpr int kBufs = 3;
+  static constexpr size_t kChunkBytes = 64u << 20;
+  std::once_flag once;
+  fftoc_status status = FFTOC_OK;
+  std::string error;
+  std::mutex mu;
+  cudaStream_t s_h2d = nullptr, s_cmp = nullptr, s_d2h = nullptr;
+  void* buf[kBufs] = {};
+  cudaEvent_t ev_h2d[kBufs] = {}, ev_cmp[kBufs] = {}, ev_d2h[kBufs] = {};
+  cudaEvent_t ev_start = nullptr;
+};
+
 struct DeviceState {
+  Staging staging;
   std::once_flag once;
   fftoc_status init_status = FFTOC_OK;
   std::string init_error;
@@ -159,6 +175,23 @@ fftoc_status device_state(DeviceState** out) {
   return FFTOC_OK;
 }
 
+void init_staging(Staging& sg) {
+  auto bad = [&](cudaError_t e, const char* what) {
+    cudaGetLastError();
+    sg.status = (e == cudaErrorMemoryAllocation) ? FFTOC_ERR_NO_MEMORY : FFTOC_ERR_CUDA;
+    sg.error = std::string(what) + ": " + cudaGetErrorString(e);
+  };
+  cudaError_t e;
+  for (cudaStream_t* st : {&sg.s_h2d, &sg.s_cmp, &sg.s_d2h})
+    if ((e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking)) != cudaSuccess) return bad(e, "cudaStreamCreate");
+  for (int b = 0; b < Staging::kBufs; ++b) {
+    if ((e = cudaMalloc(&sg.buf[b], Staging::kChunkBytes)) != cudaSuccess) return bad(e, "cudaMalloc(staging)");
+    for (cudaEvent_t* ev : {&sg.ev_h2d[b], &sg.ev_cmp[b], &sg.ev_d2h[b]})
+      if ((e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming)) != cudaSuccess) return bad(e, "cudaEventCreate");
+  }
+  if ((e = cudaEventCreateWithFlags(&sg.ev_start, cudaEventDisableTiming)) != cudaSuccess) return bad(e, "cudaEventCreate");
+}
+
 int resolve_engine(int n, int engine) {
   (void)n;
   return engine == FFTOC_ENGINE_AUTO ? FFTOC_ENGINE_FX : engine;
@@ -194,6 +227,56 @@ fftoc_status launch_fwd(int n, const double* in, double* out, int64_t batch, int
   void* args[] = {(void*)&in2, (void*)&out2, (void*)&bl, (void*)&tw};
   cudaError_t e = cudaLaunchKernel(d.fn, dim3((unsigned)blocks), dim3(d.threads), args, (size_t)d.smem, stream);
   if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchKernel");
+  return FFTOC_OK;
+}
+
+fftoc_status launch_fwd_host(int n, const double* h_in, double* h_out, int64_t batch, int engine,
+                             cudaStream_t stream) {
+  const int idx = size_index(n);
+  if (idx < 0) return fail(FFTOC_ERR_INVALID_SIZE, "n=" + std::to_string(n) + " is not one of 8,16,...,4096");
+  if (batch < 0) return fail(FFTOC_ERR_INVALID_VALUE, "batch must be >= 0");
+  if (engine < FFTOC_ENGINE_AUTO || engine > FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_INVALID_VALUE, "unknown engine");
+  if (batch == 0) return FFTOC_OK;
+  if (!h_in || !h_out) return fail(FFTOC_ERR_INVALID_VALUE, "null buffer");
+  if (((uintptr_t)h_in & 15) || ((uintptr_t)h_out & 15)) return fail(FFTOC_ERR_MISALIGNED, "buffers must be 16-byte aligned");
+  if (batch > INT64_MAX / ((int64_t)n * 16)) return fail(FFTOC_ERR_INVALID_VALUE, "batch*n overflows");
+  const uintptr_t bytes = (uintptr_t)batch * (uintptr_t)n * 16u;
+  const uintptr_t a = (uintptr_t)h_in, b = (uintptr_t)h_out;
+  if (a != b && a < b + bytes && b < a + bytes) return fail(FFTOC_ERR_INVALID_VALUE, "in and out overlap partially");
+  DeviceState* ds = nullptr;
+  fftoc_status st = device_state(&ds);
+  if (st != FFTOC_OK) return st;
+  Staging& sg = ds->staging;
+  std::call_once(sg.once, [&] { init_staging(sg); });
+  if (sg.status != FFTOC_OK) return fail(sg.status, sg.error);
+
+  std::lock_guard<std::mutex> lock(sg.mu);
+  const int64_t chunk = (int64_t)(Staging::kChunkBytes / ((size_t)n * 16));
+  cudaError_t e;
+  if ((e = cudaEventRecord(sg.ev_start, stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+  if ((e = cudaStreamWaitEvent(sg.s_h2d, sg.ev_start, 0)) != cudaSuccess) return cuda_fail(e, "cudaStreamWaitEvent");
+  int last = 0;
+  for (int64_t off = 0, c = 0; off < batch; off += chunk, ++c) {
+    const int bi = (int)(c % Staging::kBufs);
+    const int64_t cnt = (batch - off) < chunk ? (batch - off) : chunk;
+    const size_t nb = (size_t)cnt * (size_t)n * 16;
+    const char* src = reinterpret_cast<const char*>(h_in) + (size_t)off * (size_t)n * 16;
+    char* dst = reinterpret_cast<char*>(h_out) + (size_t)off * (size_t)n * 16;
+    if ((e = cudaStreamWaitEvent(sg.s_h2d, sg.ev_d2h[bi], 0)) != cudaSuccess) return cuda_fail(e, "cudaStreamWaitEvent");
+    if ((e = cudaMemcpyAsync(sg.buf[bi], src, nb, cudaMemcpyHostToDevice, sg.s_h2d)) != cudaSuccess)
+      return cuda_fail(e, "cudaMemcpyAsync(H2D)");
+    if ((e = cudaEventRecord(sg.ev_h2d[bi], sg.s_h2d)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+    if ((e = cudaStreamWaitEvent(sg.s_cmp, sg.ev_h2d[bi], 0)) != cudaSuccess) return cuda_fail(e, "cudaStreamWaitEvent");
+    st = launch_fwd(n, static_cast<const double*>(sg.buf[bi]), static_cast<double*>(sg.buf[bi]), cnt, engine, sg.s_cmp);
+    if (st != FFTOC_OK) return st;
+    if ((e = cudaEventRecord(sg.ev_cmp[bi], sg.s_cmp)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+    if ((e = cudaStreamWaitEvent(sg.s_d2h, sg.ev_cmp[bi], 0)) != cudaSuccess) return cuda_fail(e, "cudaStreamWaitEvent");
+    if ((e = cudaMemcpyAsync(dst, sg.buf[bi], nb, cudaMemcpyDeviceToHost, sg.s_d2h)) != cudaSuccess)
+      return cuda_fail(e, "cudaMemcpyAsync(D2H)");
+    if ((e = cudaEventRecord(sg.ev_d2h[bi], sg.s_d2h)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+    last = bi;
+  }
+  if ((e = cudaStreamWaitEvent(stream, sg.ev_d2h[last], 0)) != cudaSuccess) return cuda_fail(e, "cudaStreamWaitEvent");
   return FFTOC_OK;
 }
 
@@ -243,6 +326,10 @@ fftoc_status fftoc_c2c_fwd(int n, const double* in, double* out, int64_t batch, 
 
 fftoc_status fftoc_c2c_fwd_ex(int n, const double* in, double* out, int64_t batch, int engine, fftoc_stream s) {
   return fftoc::launch_fwd(n, in, out, batch, engine, (cudaStream_t)s);
+}
+
+fftoc_status fftoc_c2c_fwd_host(int n, const double* h_in, double* h_out, int64_t batch, int engine, fftoc_stream s) {
+  return fftoc::launch_fwd_host(n, h_in, h_out, batch, engine, (cudaStream_t)s);
 }
 
 fftoc_status fftoc_plan_query(int n, int engine, fftoc_plan_info* info) { return fftoc::plan_query(n, engine, info); }

@@ -63,7 +63,7 @@ typedef enum {
   FFTOC_ENGINE_AUTO = 0, /* fastest engine of the FP64 form for this n           */
   FFTOC_ENGINE_F64 = 1,  /* IEEE binary64 (DFMA/DADD)                            */
   FFTOC_ENGINE_FX = 2,   /* 64-bit block fixed point: per-transform power-of-two
-                            scale, exact integer adds, 62-bit twiddles;
+                            scale, exact integer adds, 60-bit twiddles;
                             relative L2 error ~1e-15                             */
   FFTOC_ENGINE_DMMA = 3  /* Karatsuba complex GEMM on FP64 mma.m8n8k4
                             (the reference's tensor_utils.cuh:32-36 scheme)      */
@@ -90,6 +90,21 @@ fftoc_status fftoc_c2c_fwd(int n, const double *in, double *out, int64_t batch, 
 /* Same, with an explicit engine. */
 fftoc_status fftoc_c2c_fwd_ex(int n, const double *in, double *out, int64_t batch, int engine,
                               fftoc_stream stream);
+
+/* Host buffers in and out (the reference harness's path: cudaMemcpy H2D,
+ * launch, cudaMemcpy D2H — includes/testing.cuh:109-113,166-171).
+ * h_in/h_out are HOST pointers (pinned memory gives overlapped, full-speed
+ * copies; pageable memory works but copies synchronously), 16-byte aligned,
+ * batch*n complex values each; h_in == h_out is allowed.  The batch is
+ * streamed through the device in chunks of 64 MiB (H2D, transform and D2H
+ * of consecutive chunks overlap on three internal streams).  The call is
+ * ordered after earlier work on `stream` and `stream` is ordered after its
+ * last copy: synchronise `stream` before reading h_out.  The first call on a
+ * device allocates 192 MiB of device staging memory and the streams (make it
+ * before any stream capture); calls from several host threads serialise
+ * their enqueueing. */
+fftoc_status fftoc_c2c_fwd_host(int n, const double *h_in, double *h_out, int64_t batch, int engine,
+                                fftoc_stream stream);
 
 /* Launch geometry of a size/engine (reference: the FFTExec static members
  * threads / units_per_block / ffts_per_unit, e.g. tensor_fft_64.cuh:16-19). */
