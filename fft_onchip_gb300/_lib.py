@@ -32,6 +32,9 @@ EXPORTS = tuple(["fftoc_c2c_fwd_n%d" % n for n in SIZES]) + (
     "fftoc_c2c_fwd_ex",
     "fftoc_c2c_fwd_host",
     "fftoc_plan_query",
+    "fftoc_plan_query_variant",
+    "fftoc_plan_select",
+    "fftoc_autotune",
     "fftoc_auto_engine",
     "fftoc_status_string",
     "fftoc_last_error_string",
@@ -49,6 +52,9 @@ class PlanInfo(ctypes.Structure):
         ("smem_bytes", ctypes.c_int),
         ("passes", ctypes.c_int),
         ("radix", ctypes.c_int * 4),
+        ("points_per_thread", ctypes.c_int),
+        ("variant", ctypes.c_int),
+        ("variants", ctypes.c_int),
     ]
 
 
@@ -84,6 +90,12 @@ def load(path=None):
     L.fftoc_c2c_fwd_host.restype = c_int
     L.fftoc_plan_query.argtypes = [c_int, c_int, ctypes.POINTER(PlanInfo)]
     L.fftoc_plan_query.restype = c_int
+    L.fftoc_plan_query_variant.argtypes = [c_int, c_int, c_int, ctypes.POINTER(PlanInfo)]
+    L.fftoc_plan_query_variant.restype = c_int
+    L.fftoc_plan_select.argtypes = [c_int, c_int, c_int]
+    L.fftoc_plan_select.restype = c_int
+    L.fftoc_autotune.argtypes = [c_int, c_int, i64, vp, ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_float)]
+    L.fftoc_autotune.restype = c_int
     L.fftoc_auto_engine.argtypes = [c_int]
     L.fftoc_auto_engine.restype = c_int
     L.fftoc_status_string.argtypes = [c_int]
@@ -103,9 +115,7 @@ def check(status):
     return status
 
 
-def plan_query(n, engine=ENGINE_AUTO):
-    info = PlanInfo()
-    check(load().fftoc_plan_query(int(n), int(engine), ctypes.byref(info)))
+def _info_dict(info):
     return {
         "n": info.n,
         "engine": info.engine,
@@ -115,4 +125,29 @@ def plan_query(n, engine=ENGINE_AUTO):
         "smem_bytes": info.smem_bytes,
         "passes": info.passes,
         "radix": [info.radix[i] for i in range(info.passes)],
+        "points_per_thread": info.points_per_thread,
+        "variant": info.variant,
+        "variants": info.variants,
     }
+
+
+def plan_query(n, engine=ENGINE_AUTO, variant=None):
+    """Plan in use for (n, engine), or compiled plan `variant`."""
+    info = PlanInfo()
+    if variant is None:
+        check(load().fftoc_plan_query(int(n), int(engine), ctypes.byref(info)))
+    else:
+        check(load().fftoc_plan_query_variant(int(n), int(engine), int(variant), ctypes.byref(info)))
+    return _info_dict(info)
+
+
+def plan_select(n, engine, variant):
+    check(load().fftoc_plan_select(int(n), int(engine), int(variant)))
+
+
+def autotune(n, engine, batch, stream_ptr=0):
+    """Time every compiled plan; select and return (variant, ms per launch)."""
+    best = ctypes.c_int()
+    ms = ctypes.c_float()
+    check(load().fftoc_autotune(int(n), int(engine), int(batch), stream_ptr, ctypes.byref(best), ctypes.byref(ms)))
+    return best.value, ms.value

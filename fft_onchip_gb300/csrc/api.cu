@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -93,16 +94,28 @@ struct DeviceState {
   std::once_flag once;
   fftoc_status init_status = FFTOC_OK;
   std::string init_error;
-  KernelDesc f64[kNumSizes];
-  KernelDesc fx[kNumSizes];
-  void* tw_f64[kNumSizes] = {};
-  void* tw_fx[kNumSizes] = {};
+  SizeVariants var[2][kNumSizes];                 // [engine: 0 f64, 1 fx][size]
+  void* tw[2][kNumSizes][kMaxVariants] = {};      // per-variant twiddle tables
 };
+
+// Plan chosen per (engine, size): process-wide, set by fftoc_plan_select or
+// fftoc_autotune; variant 0 until then.
+std::atomic<int> g_choice[2][kNumSizes];
+
+const SizeVariants* host_variants(int eng_slot) {
+  static SizeVariants table[2][kNumSizes];
+  static std::once_flag once;
+  std::call_once(once, [] {
+    describe_f64(table[0]);
+    describe_fx(table[1]);
+  });
+  return table[eng_slot];
+}
 
 constexpr int kMaxDevices = 64;
 DeviceState g_devices[kMaxDevices];
 
-void build_twiddles(const KernelDesc& d, int n, std::vector<double>& f64, std::vector<int>& fx) {
+void build_twiddles(const KernelDesc& d, std::vector<double>& f64, std::vector<int>& fx) {
   f64.assign((size_t)d.tw_entries * 2, 0.0);
   fx.assign((size_t)d.tw_entries * 4, 0);
   int off = 0, p = d.radix[0];
@@ -121,46 +134,44 @@ void build_twiddles(const KernelDesc& d, int n, std::vector<double>& f64, std::v
     off += (R - 1) * p;
     p *= R;
   }
-  (void)n;
 }
 
 void init_device(DeviceState& ds) {
-  describe_f64(ds.f64);
-  describe_fx(ds.fx);
-  for (int i = 0; i < kNumSizes; ++i) {
-    for (KernelDesc* d : {&ds.f64[i], &ds.fx[i]}) {
-      cudaError_t e = cudaFuncSetAttribute(d->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, d->smem);
-      if (e != cudaSuccess) {
-        cudaGetLastError();
-        ds.init_status = FFTOC_ERR_CUDA;
-        ds.init_error = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
-        return;
+  for (int eng = 0; eng < 2; ++eng)
+    for (int i = 0; i < kNumSizes; ++i) ds.var[eng][i] = host_variants(eng)[i];
+  for (int eng = 0; eng < 2; ++eng)
+    for (int i = 0; i < kNumSizes; ++i)
+      for (int v = 0; v < ds.var[eng][i].count; ++v) {
+        const KernelDesc& d = ds.var[eng][i].v[v];
+        cudaError_t e = cudaFuncSetAttribute(d.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, d.smem);
+        if (e != cudaSuccess) {
+          cudaGetLastError();
+          ds.init_status = FFTOC_ERR_CUDA;
+          ds.init_error = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
+          return;
+        }
+        std::vector<double> f64;
+        std::vector<int> fx;
+        build_twiddles(d, f64, fx);
+        const size_t bytes = (size_t)(d.tw_entries > 0 ? d.tw_entries : 1) * 16;
+        void* p = nullptr;
+        e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) {
+          cudaGetLastError();
+          ds.init_status = FFTOC_ERR_NO_MEMORY;
+          ds.init_error = std::string("cudaMalloc(twiddles): ") + cudaGetErrorString(e);
+          return;
+        }
+        const void* src = eng == 0 ? (const void*)f64.data() : (const void*)fx.data();
+        if (d.tw_entries > 0) e = cudaMemcpy(p, src, (size_t)d.tw_entries * 16, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+          cudaGetLastError();
+          ds.init_status = FFTOC_ERR_CUDA;
+          ds.init_error = std::string("cudaMemcpy(twiddles): ") + cudaGetErrorString(e);
+          return;
+        }
+        ds.tw[eng][i][v] = p;
       }
-    }
-    std::vector<double> f64;
-    std::vector<int> fx;
-    build_twiddles(ds.f64[i], kSizes[i], f64, fx);
-    const size_t bytes = (size_t)(ds.f64[i].tw_entries > 0 ? ds.f64[i].tw_entries : 1) * 16;
-    for (int eng = 0; eng < 2; ++eng) {
-      void* p = nullptr;
-      cudaError_t e = cudaMalloc(&p, bytes);
-      if (e != cudaSuccess) {
-        cudaGetLastError();
-        ds.init_status = FFTOC_ERR_NO_MEMORY;
-        ds.init_error = std::string("cudaMalloc(twiddles): ") + cudaGetErrorString(e);
-        return;
-      }
-      const void* src = eng == 0 ? (const void*)f64.data() : (const void*)fx.data();
-      if (ds.f64[i].tw_entries > 0) e = cudaMemcpy(p, src, (size_t)ds.f64[i].tw_entries * 16, cudaMemcpyHostToDevice);
-      if (e != cudaSuccess) {
-        cudaGetLastError();
-        ds.init_status = FFTOC_ERR_CUDA;
-        ds.init_error = std::string("cudaMemcpy(twiddles): ") + cudaGetErrorString(e);
-        return;
-      }
-      (eng == 0 ? ds.tw_f64[i] : ds.tw_fx[i]) = p;
-    }
-  }
 }
 
 fftoc_status device_state(DeviceState** out) {
@@ -199,7 +210,8 @@ int resolve_engine(int n, int engine) {
 
 }  // namespace
 
-fftoc_status launch_fwd(int n, const double* in, double* out, int64_t batch, int engine, cudaStream_t stream) {
+fftoc_status launch_fwd(int n, const double* in, double* out, int64_t batch, int engine, cudaStream_t stream,
+                        int variant = -1) {
   const int idx = size_index(n);
   if (idx < 0) return fail(FFTOC_ERR_INVALID_SIZE, "n=" + std::to_string(n) + " is not one of 8,16,...,4096");
   if (batch < 0) return fail(FFTOC_ERR_INVALID_VALUE, "batch must be >= 0");
@@ -217,8 +229,11 @@ fftoc_status launch_fwd(int n, const double* in, double* out, int64_t batch, int
   DeviceState* ds = nullptr;
   fftoc_status st = device_state(&ds);
   if (st != FFTOC_OK) return st;
-  const KernelDesc& d = eng == FFTOC_ENGINE_FX ? ds->fx[idx] : ds->f64[idx];
-  const void* tw = eng == FFTOC_ENGINE_FX ? ds->tw_fx[idx] : ds->tw_f64[idx];
+  const int slot = eng == FFTOC_ENGINE_FX ? 1 : 0;
+  const int var = variant >= 0 ? variant : g_choice[slot][idx].load(std::memory_order_relaxed);
+  if (var >= ds->var[slot][idx].count) return fail(FFTOC_ERR_INVALID_VALUE, "no such plan variant");
+  const KernelDesc& d = ds->var[slot][idx].v[var];
+  const void* tw = ds->tw[slot][idx][var];
   const long long blocks = (batch + d.tpb - 1) / d.tpb;
   if (blocks > 0x7FFFFFFFLL) return fail(FFTOC_ERR_INVALID_VALUE, "batch too large for one launch");
   const double2* in2 = reinterpret_cast<const double2*>(in);
@@ -280,23 +295,91 @@ fftoc_status launch_fwd_host(int n, const double* h_in, double* h_out, int64_t b
   return FFTOC_OK;
 }
 
-fftoc_status plan_query(int n, int engine, fftoc_plan_info* info) {
+fftoc_status plan_query(int n, int engine, int variant, fftoc_plan_info* info) {
   const int idx = size_index(n);
   if (idx < 0) return fail(FFTOC_ERR_INVALID_SIZE, "n=" + std::to_string(n) + " is not one of 8,16,...,4096");
   if (!info) return fail(FFTOC_ERR_INVALID_VALUE, "null info");
   if (engine < FFTOC_ENGINE_AUTO || engine > FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_INVALID_VALUE, "unknown engine");
   const int eng = resolve_engine(n, engine);
   if (eng == FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_UNSUPPORTED, "DMMA engine not available for n=" + std::to_string(n));
-  KernelDesc d[kNumSizes];
-  if (eng == FFTOC_ENGINE_FX) describe_fx(d); else describe_f64(d);
+  const int slot = eng == FFTOC_ENGINE_FX ? 1 : 0;
+  const SizeVariants& sv = host_variants(slot)[idx];
+  const int var = variant >= 0 ? variant : g_choice[slot][idx].load(std::memory_order_relaxed);
+  if (var >= sv.count) return fail(FFTOC_ERR_INVALID_VALUE, "no such plan variant");
+  const KernelDesc& d = sv.v[var];
   info->n = n;
   info->engine = eng;
-  info->threads_per_transform = d[idx].tpt;
-  info->transforms_per_block = d[idx].tpb;
-  info->threads_per_block = d[idx].threads;
-  info->smem_bytes = d[idx].smem;
-  info->passes = d[idx].passes;
-  for (int i = 0; i < 4; ++i) info->radix[i] = d[idx].radix[i];
+  info->threads_per_transform = d.tpt;
+  info->transforms_per_block = d.tpb;
+  info->threads_per_block = d.threads;
+  info->smem_bytes = d.smem;
+  info->passes = d.passes;
+  for (int i = 0; i < 4; ++i) info->radix[i] = d.radix[i];
+  info->points_per_thread = d.ppt;
+  info->variant = var;
+  info->variants = sv.count;
+  return FFTOC_OK;
+}
+
+fftoc_status plan_select(int n, int engine, int variant) {
+  fftoc_plan_info info;
+  fftoc_status st = plan_query(n, engine, variant < 0 ? 0 : variant, &info);
+  if (st != FFTOC_OK) return st;
+  if (variant < 0) return fail(FFTOC_ERR_INVALID_VALUE, "variant must be >= 0");
+  g_choice[info.engine == FFTOC_ENGINE_FX ? 1 : 0][size_index(n)].store(variant);
+  return FFTOC_OK;
+}
+
+// Time every compiled plan of (n, engine) on a device scratch batch of
+// `batch` transforms (3 warm-up + 5 timed launches each, on `stream`), select
+// the fastest and report it.  Synchronous; allocates and frees the scratch.
+fftoc_status autotune(int n, int engine, int64_t batch, cudaStream_t stream, int* best_variant, float* best_ms) {
+  fftoc_plan_info info;
+  fftoc_status st = plan_query(n, engine, 0, &info);
+  if (st != FFTOC_OK) return st;
+  if (batch <= 0) return fail(FFTOC_ERR_INVALID_VALUE, "batch must be > 0");
+  if (batch > INT64_MAX / ((int64_t)n * 16)) return fail(FFTOC_ERR_INVALID_VALUE, "batch*n overflows");
+  const size_t bytes = (size_t)batch * (size_t)n * 16;
+  void *x = nullptr, *y = nullptr;
+  cudaError_t e = cudaMalloc(&x, bytes);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(autotune)");
+  e = cudaMalloc(&y, bytes);
+  if (e != cudaSuccess) {
+    cudaFree(x);
+    return cuda_fail(e, "cudaMalloc(autotune)");
+  }
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = 1e30f;
+  int bestv = 0;
+  // deterministic non-trivial input: bytes 0x3F.. give doubles near 0.5
+  e = cudaMemsetAsync(x, 0x3F, bytes, stream);
+  for (int v = 0; v < info.variants && e == cudaSuccess && st == FFTOC_OK; ++v) {
+    for (int r = 0; r < 3 && st == FFTOC_OK; ++r)
+      st = launch_fwd(n, (const double*)x, (double*)y, batch, info.engine, stream, v);
+    if (st != FFTOC_OK) break;
+    cudaEventRecord(a, stream);
+    for (int r = 0; r < 5 && st == FFTOC_OK; ++r)
+      st = launch_fwd(n, (const double*)x, (double*)y, batch, info.engine, stream, v);
+    cudaEventRecord(b, stream);
+    e = cudaEventSynchronize(b);
+    float ms = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    if (e == cudaSuccess && ms / 5 < best) {
+      best = ms / 5;
+      bestv = v;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(x);
+  cudaFree(y);
+  if (st != FFTOC_OK) return st;
+  if (e != cudaSuccess) return cuda_fail(e, "autotune");
+  g_choice[info.engine == FFTOC_ENGINE_FX ? 1 : 0][size_index(n)].store(bestv);
+  if (best_variant) *best_variant = bestv;
+  if (best_ms) *best_ms = best;
   return FFTOC_OK;
 }
 
@@ -332,7 +415,17 @@ fftoc_status fftoc_c2c_fwd_host(int n, const double* h_in, double* h_out, int64_
   return fftoc::launch_fwd_host(n, h_in, h_out, batch, engine, (cudaStream_t)s);
 }
 
-fftoc_status fftoc_plan_query(int n, int engine, fftoc_plan_info* info) { return fftoc::plan_query(n, engine, info); }
+fftoc_status fftoc_plan_query(int n, int engine, fftoc_plan_info* info) { return fftoc::plan_query(n, engine, -1, info); }
+
+fftoc_status fftoc_plan_query_variant(int n, int engine, int variant, fftoc_plan_info* info) {
+  return fftoc::plan_query(n, engine, variant, info);
+}
+
+fftoc_status fftoc_plan_select(int n, int engine, int variant) { return fftoc::plan_select(n, engine, variant); }
+
+fftoc_status fftoc_autotune(int n, int engine, int64_t batch, fftoc_stream s, int* best_variant, float* best_ms) {
+  return fftoc::autotune(n, engine, batch, (cudaStream_t)s, best_variant, best_ms);
+}
 
 int fftoc_auto_engine(int n) { return fftoc::size_index(n) < 0 ? -1 : FFTOC_ENGINE_FX; }
 

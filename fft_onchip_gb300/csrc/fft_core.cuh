@@ -26,36 +26,37 @@
 namespace fftoc {
 
 // ---------------------------------------------------------------------------
-// Plans: points per thread P and the radix of each pass (product = N).
+// Plans: a transform of N points is split over T = N/P threads holding P
+// points each, and computed in passes of radix R[0], R[1], ... (product N,
+// every R dividing P).  T threads per transform, TPB transforms per CTA.
 // ---------------------------------------------------------------------------
-template <int N> struct Plan;
-template <> struct Plan<8>    { static constexpr int P = 8,  S = 1; static constexpr int R[4] = {8, 1, 1, 1}; };
-template <> struct Plan<16>   { static constexpr int P = 16, S = 1; static constexpr int R[4] = {16, 1, 1, 1}; };
-template <> struct Plan<32>   { static constexpr int P = 8,  S = 2; static constexpr int R[4] = {8, 4, 1, 1}; };
-template <> struct Plan<64>   { static constexpr int P = 8,  S = 2; static constexpr int R[4] = {8, 8, 1, 1}; };
-template <> struct Plan<128>  { static constexpr int P = 16, S = 2; static constexpr int R[4] = {16, 8, 1, 1}; };
-template <> struct Plan<256>  { static constexpr int P = 16, S = 2; static constexpr int R[4] = {16, 16, 1, 1}; };
-template <> struct Plan<512>  { static constexpr int P = 8,  S = 3; static constexpr int R[4] = {8, 8, 8, 1}; };
-template <> struct Plan<1024> { static constexpr int P = 16, S = 3; static constexpr int R[4] = {16, 8, 8, 1}; };
-template <> struct Plan<2048> { static constexpr int P = 16, S = 3; static constexpr int R[4] = {16, 16, 8, 1}; };
-template <> struct Plan<4096> { static constexpr int P = 8,  S = 4; static constexpr int R[4] = {8, 8, 8, 8}; };
-
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
-// span p of pass s (product of the radices before it)
-template <int N> __host__ __device__ constexpr int span_of(int s) {
-  int p = 1;
-  for (int i = 0; i < s; ++i) p *= Plan<N>::R[i];
-  return p;
-}
-// offset (in twiddle entries) of pass s's table; pass s holds (R-1)*p entries,
-// entry (m-1)*p + k = W_{R p}^{k m}.  Pass 0 has no twiddles.
-template <int N> __host__ __device__ constexpr int tw_offset(int s) {
-  int off = 0;
-  for (int i = 1; i < s; ++i) off += (Plan<N>::R[i] - 1) * span_of<N>(i);
-  return off;
-}
-template <int N> __host__ __device__ constexpr int tw_count() { return tw_offset<N>(Plan<N>::S); }
+template <int N_, int P_, int TPB_, int R0, int R1 = 1, int R2 = 1, int R3 = 1>
+struct PlanT {
+  static constexpr int N = N_;
+  static constexpr int P = P_;
+  static constexpr int TPB = TPB_;
+  static constexpr int R[4] = {R0, R1, R2, R3};
+  static constexpr int S = (R0 > 1) + (R1 > 1) + (R2 > 1) + (R3 > 1);
+  static constexpr int T = N / P;
+  static_assert(R0 * R1 * R2 * R3 == N, "radices must multiply to N");
+  static_assert(P % R0 == 0 && P % R1 == 0 && P % R2 == 0 && P % R3 == 0, "every radix divides P");
+  // span p of pass s (product of the radices before it)
+  __host__ __device__ static constexpr int span(int s) {
+    int p = 1;
+    for (int i = 0; i < s; ++i) p *= R[i];
+    return p;
+  }
+  // offset (in twiddle entries) of pass s's table; pass s holds (R-1)*p
+  // entries, entry (m-1)*p + k = W_{R p}^{k m}.  Pass 0 has no twiddles.
+  __host__ __device__ static constexpr int tw_offset(int s) {
+    int off = 0;
+    for (int i = 1; i < s; ++i) off += (R[i] - 1) * span(i);
+    return off;
+  }
+  static constexpr int TW_COUNT = tw_offset(S);
+};
 
 // ---------------------------------------------------------------------------
 // Engines

@@ -59,15 +59,23 @@ FFTOC_HD long long fx_in(unsigned hw, unsigned lw, int eref) {
   return ((int)hw < 0) ? -r : r;
 }
 
-// x * 2^K, K = Emax - 1022 - B.  Fast path adds K to the exponent field of the
-// correctly rounded conversion (exact); `slow` transforms (result exponents
-// outside the normal range) use ldexp.
-FFTOC_HD double fx_out(long long x, int kshift, int K, bool slow) {
+// x * 2^K, K = Emax - 1022 - B: the correctly rounded conversion with K added
+// to its exponent field (exact).  Valid while every result exponent stays in
+// the normal range (fx_scale's `slow` is false); one FP64-pipe instruction.
+FFTOC_HD double fx_out(long long x, int kshift) {
   const double d = (double)x;
-  if (slow) return ldexp(d, K);
   const unsigned hi = hi_word(d);
   return from_words(x != 0 ? hi + (unsigned)kshift : hi, lo_word(d));
 }
+
+// Transforms whose outputs may be subnormal or overflow: ldexp.  Kept out of
+// line so the compiler cannot if-convert it into the fast path (predicated-off
+// FP64 instructions would still occupy the FP64 pipe).
+#ifdef __CUDA_ARCH__
+__device__ __noinline__ double fx_out_slow(long long x, int K) { return ldexp((double)x, K); }
+#else
+inline double fx_out_slow(long long x, int K) { return ldexp((double)x, K); }
+#endif
 
 // Scale parameters of a transform from its largest biased exponent.
 struct FxScale {
@@ -86,14 +94,16 @@ FFTOC_HD FxScale fx_scale(int em) {
 }
 
 // --- the kernel ---------------------------------------------------------------
-template <class E, int N, int TPB>
+template <class E, class PL>
 struct Fft {
   using S = typename E::S;
   using TW = typename E::TW;
-  static constexpr int P = Plan<N>::P;
-  static constexpr int T = N / P;
-  static constexpr int NS = Plan<N>::S;
-  static constexpr int SW = ilog2c(Plan<N>::R[0]);
+  static constexpr int N = PL::N;
+  static constexpr int TPB = PL::TPB;
+  static constexpr int P = PL::P;
+  static constexpr int T = PL::T;
+  static constexpr int NS = PL::S;
+  static constexpr int SW = ilog2c(PL::R[0]) < 3 ? 3 : ilog2c(PL::R[0]);
   static constexpr int THREADS = T * TPB;
   static constexpr bool STAGED = T < 8;  // small N: stage HBM tiles through smem
   static constexpr int SMEM = TPB * N * 16 + 64;
@@ -105,13 +115,13 @@ struct Fft {
 
   template <int s, int b>
   __device__ __forceinline__ static void butterfly(S (&re)[P], S (&im)[P], int t, const TW* __restrict__ tw) {
-    constexpr int R = Plan<N>::R[s];
+    constexpr int R = PL::R[s];
     constexpr int B = P / R;
-    constexpr int p = span_of<N>(s);
+    constexpr int p = PL::span(s);
     if constexpr (s > 0) {
       const int tp = t + T * b;
       const int k = tp & (p - 1);
-      const TW* base = tw + tw_offset<N>(s) + k;
+      const TW* base = tw + PL::tw_offset(s) + k;
 #pragma unroll
       for (int m = 1; m < R; ++m) {
         const TW w = __ldg(base + (m - 1) * p);
@@ -130,8 +140,8 @@ struct Fft {
   // destination index of output m of butterfly b in pass s
   template <int s>
   __device__ __forceinline__ static int dest(int t, int b, int m) {
-    constexpr int R = Plan<N>::R[s];
-    constexpr int p = span_of<N>(s);
+    constexpr int R = PL::R[s];
+    constexpr int p = PL::span(s);
     const int tp = t + T * b;
     const int k = tp & (p - 1);
     return (tp - k) * R + k + m * p;
@@ -139,7 +149,7 @@ struct Fft {
 
   template <int s>
   __device__ __forceinline__ static void write_smem(S (&re)[P], S (&im)[P], int j, int t, longlong2* sm) {
-    constexpr int R = Plan<N>::R[s];
+    constexpr int R = PL::R[s];
     constexpr int B = P / R;
 #pragma unroll
     for (int b = 0; b < B; ++b)
@@ -172,7 +182,7 @@ struct Fft {
   template <int s>
   __device__ __forceinline__ static void run_passes(S (&re)[P], S (&im)[P], int j, int t, const TW* __restrict__ tw,
                                                     longlong2* sm) {
-    constexpr int R = Plan<N>::R[s];
+    constexpr int R = PL::R[s];
     pass<s>(re, im, t, tw, std::make_integer_sequence<int, P / R>{});
     if constexpr (s + 1 < NS) {
       if constexpr (s > 0) __syncthreads();  // previous readers of the buffer are done
@@ -186,12 +196,13 @@ struct Fft {
 
 // Engine-specific entry/exit: load raw points (binary64), convert, run the
 // passes, convert back and store.
-template <class E, int N, int TPB>
-__global__ void __launch_bounds__(Fft<E, N, TPB>::THREADS)
+template <class E, class PL>
+__global__ void __launch_bounds__(Fft<E, PL>::THREADS)
 fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long long batch,
                const typename E::TW* __restrict__ tw) {
-  using F = Fft<E, N, TPB>;
+  using F = Fft<E, PL>;
   using S = typename E::S;
+  constexpr int N = PL::N, TPB = PL::TPB;
   constexpr int P = F::P, T = F::T, NS = F::NS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   longlong2* sm = reinterpret_cast<longlong2*>(smem_raw);
@@ -227,7 +238,7 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
 
   S re[P], im[P];
   int K = 0, kshift = 0;
-  bool slow = false, special = false;
+  bool slow = false, special = false, slow_bits = false;
   if constexpr (E::kId == EngF64::kId) {
 #pragma unroll
     for (int i = 0; i < P; ++i) { re[i] = raw[i].x; im[i] = raw[i].y; }
@@ -268,19 +279,32 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
   F::template run_passes<0>(re, im, j, t, tw, sm);
 
   // ---- store: output m of butterfly b of the last pass is element dest(...)
-  constexpr int RL = Plan<N>::R[NS - 1];
+  constexpr int RL = PL::R[NS - 1];
   constexpr int BL = P / RL;
   auto result = [&](int i) -> double2 {
     if constexpr (E::kId == EngF64::kId) {
       return make_double2(re[i], im[i]);
     } else {
-      if (special) {
-        const double qnan = __longlong_as_double(0x7FF8000000000000LL);
-        return make_double2(qnan, qnan);
-      }
-      return make_double2(fx_out((long long)re[i], kshift, K, slow), fx_out((long long)im[i], kshift, K, slow));
+      if (slow_bits) return make_double2(__longlong_as_double(re[i]), __longlong_as_double(im[i]));
+      return make_double2(fx_out((long long)re[i], kshift), fx_out((long long)im[i], kshift));
     }
   };
+  if constexpr (E::kId == EngFx::kId) {
+    // rare transforms (outputs outside the normal range, or non-finite
+    // inputs): convert in place on the slow path, then store as usual
+    if (slow || special) {
+      const double qnan = __longlong_as_double(0x7FF8000000000000LL);
+#pragma unroll
+      for (int i = 0; i < P; ++i) {
+        const double r = special ? qnan : fx_out_slow((long long)re[i], K);
+        const double m = special ? qnan : fx_out_slow((long long)im[i], K);
+        re[i] = __double_as_longlong(r);
+        im[i] = __double_as_longlong(m);
+      }
+      kshift = 0;
+      slow_bits = true;
+    }
+  }
   if constexpr (F::STAGED) {
     if constexpr (NS > 1) __syncthreads();
 #pragma unroll

@@ -14,32 +14,28 @@ inline int size_index(int n) {
   return -1;
 }
 
-// Transforms per CTA for the register/shared-memory kernels (about 256 threads
-// per CTA, at most 64 KiB of shared memory).
-constexpr int tpb_of(int n) {
-  return n == 8 ? 256 : n == 16 ? 256 : n == 32 ? 64 : n == 64 ? 32 : n == 128 ? 32 : n == 256 ? 16
-       : n == 512 ? 4 : n == 1024 ? 4 : n == 2048 ? 2 : 1;
-}
-
-// Per-size launch description filled by the engine translation units.
+// One compiled kernel (an engine x plan instantiation).
 struct KernelDesc {
-  const void* fn = nullptr;     // __global__ function
-  int threads = 0;              // threads per CTA
-  int tpb = 0;                  // transforms per CTA
-  int smem = 0;                 // dynamic shared memory bytes
-  int tpt = 0;                  // threads per transform
+  const void* fn = nullptr;  // __global__ function
+  int threads = 0;           // threads per CTA
+  int tpb = 0;               // transforms per CTA
+  int smem = 0;              // dynamic shared memory bytes
+  int tpt = 0;               // threads per transform
+  int ppt = 0;               // points per thread
   int passes = 0;
   int radix[4] = {1, 1, 1, 1};
-  int tw_entries = 0;           // twiddle table entries (16 bytes each)
+  int tw_entries = 0;        // twiddle table entries (16 bytes each)
 };
 
-// Fill `desc[kNumSizes]` for an engine (implemented in kernels_<engine>.cu).
-void describe_f64(KernelDesc* desc);
-void describe_fx(KernelDesc* desc);
-
-// Twiddle tables (api.cu): entry (m-1)*p + k of pass s = W_{R p}^{k m}.
-struct TwiddleSet {
-  void* dev[kNumSizes] = {};  // device pointer per size
+constexpr int kMaxVariants = 4;
+struct SizeVariants {
+  int count = 0;
+  KernelDesc v[kMaxVariants];
 };
+
+// Fill `per_size[kNumSizes]` with the compiled plans of an engine
+// (kernels_<engine>.cu); variant 0 is the default choice.
+void describe_f64(SizeVariants* per_size);
+void describe_fx(SizeVariants* per_size);
 
 }  // namespace fftoc

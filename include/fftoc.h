@@ -117,9 +117,30 @@ typedef struct {
   int smem_bytes;             /* dynamic shared memory per CTA               */
   int passes;                 /* Stockham passes                             */
   int radix[4];               /* radix of each pass                          */
+  int points_per_thread;
+  int variant;                /* index of this plan among the compiled ones  */
+  int variants;               /* number of compiled plans for (n, engine)    */
 } fftoc_plan_info;
 
+/* Plan currently used for (n, engine). */
 fftoc_status fftoc_plan_query(int n, int engine, fftoc_plan_info *info);
+
+/* Any compiled plan of (n, engine), 0 <= variant < info.variants. */
+fftoc_status fftoc_plan_query_variant(int n, int engine, int variant, fftoc_plan_info *info);
+
+/* Use plan `variant` for (n, engine) from now on (process-wide).  The
+ * reference picks executor parameters (UPB, FPU) at compile time through the
+ * generated sweep, scripts/generate_bench.py:93-113; here the choice is made
+ * at run time among the compiled plans. */
+fftoc_status fftoc_plan_select(int n, int engine, int variant);
+
+/* Autotuner: time every compiled plan of (n, engine) on a scratch batch of
+ * `batch` transforms, select the fastest and return its index and time per
+ * launch (ms).  Synchronous on `stream`; allocates and frees 2*batch*n*16
+ * bytes of device scratch.  (Reference: the manual sweep of
+ * scripts/generate_bench.py:93-113 and src/saturation.cu:36-44.) */
+fftoc_status fftoc_autotune(int n, int engine, int64_t batch, fftoc_stream stream, int *best_variant,
+                            float *best_ms);
 
 /* Engine that FFTOC_ENGINE_AUTO resolves to for size n. */
 int fftoc_auto_engine(int n);

@@ -107,7 +107,7 @@ static double check_conversions(std::mt19937_64& g) {
     for (int i = 0; i < 64; ++i) mx = fmax(mx, fabs(x[i]));
     for (int i = 0; i < 64; ++i) {
       const long long f = fx_in(hi_word(x[i]), lo_word(x[i]), s.eref);
-      const double y = fx_out(f, s.kshift, s.K, s.slow);
+      const double y = s.slow ? fx_out_slow(f, s.K) : fx_out(f, s.kshift);
       const double e = fabs(y - x[i]) / mx;
       if (e > worst) worst = e;
     }

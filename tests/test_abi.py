@@ -43,15 +43,34 @@ def test_version_and_status_strings(fftoc_lib):
 @pytest.mark.parametrize("n", _lib.SIZES)
 @pytest.mark.parametrize("engine", ["auto", "f64", "fx"])
 def test_plan_query(fftoc_lib, n, engine):
-    p = _lib.plan_query(n, _lib.ENGINES[engine])
-    assert p["n"] == n
-    assert p["engine"] in (_lib.ENGINE_F64, _lib.ENGINE_FX)
-    prod = 1
-    for r in p["radix"]:
-        prod *= r
-    assert prod == n
-    assert p["threads_per_transform"] * p["transforms_per_block"] == p["threads_per_block"]
-    assert p["threads_per_block"] <= 1024 and p["smem_bytes"] <= 227 * 1024
+    cur = _lib.plan_query(n, _lib.ENGINES[engine])
+    assert cur["variants"] >= 1 and 0 <= cur["variant"] < cur["variants"]
+    for v in range(cur["variants"]):
+        p = _lib.plan_query(n, _lib.ENGINES[engine], variant=v)
+        assert p["n"] == n and p["variant"] == v
+        assert p["engine"] in (_lib.ENGINE_F64, _lib.ENGINE_FX)
+        prod = 1
+        for r in p["radix"]:
+            prod *= r
+            assert p["points_per_thread"] % r == 0
+        assert prod == n
+        assert p["threads_per_transform"] * p["points_per_thread"] == n
+        assert p["threads_per_transform"] * p["transforms_per_block"] == p["threads_per_block"]
+        assert p["threads_per_block"] <= 1024 and p["smem_bytes"] <= 227 * 1024
+
+
+def test_plan_select(fftoc_lib):
+    L = fftoc_lib
+    cur = _lib.plan_query(64, _lib.ENGINE_FX)
+    nv = cur["variants"]
+    try:
+        _lib.plan_select(64, _lib.ENGINE_FX, nv - 1)
+        assert _lib.plan_query(64, _lib.ENGINE_FX)["variant"] == nv - 1
+        assert L.fftoc_plan_select(64, _lib.ENGINE_FX, nv) == 2      # out of range
+        assert L.fftoc_plan_select(64, _lib.ENGINE_FX, -1) == 2
+        assert L.fftoc_plan_select(60, _lib.ENGINE_FX, 0) == 1
+    finally:
+        _lib.plan_select(64, _lib.ENGINE_FX, cur["variant"])
 
 
 def _call(L, n, inp, out, batch, engine=0):
