@@ -35,6 +35,7 @@ EXPORTS = tuple(["fftoc_c2c_fwd_n%d" % n for n in SIZES]) + (
     "fftoc_plan_query_variant",
     "fftoc_plan_select",
     "fftoc_autotune",
+    "fftoc_device_error_check",
     "fftoc_auto_engine",
     "fftoc_status_string",
     "fftoc_last_error_string",
@@ -55,6 +56,8 @@ class PlanInfo(ctypes.Structure):
         ("points_per_thread", ctypes.c_int),
         ("variant", ctypes.c_int),
         ("variants", ctypes.c_int),
+        ("persistent", ctypes.c_int),
+        ("stages", ctypes.c_int),
     ]
 
 
@@ -96,6 +99,8 @@ def load(path=None):
     L.fftoc_plan_select.restype = c_int
     L.fftoc_autotune.argtypes = [c_int, c_int, i64, vp, ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_float)]
     L.fftoc_autotune.restype = c_int
+    L.fftoc_device_error_check.argtypes = []
+    L.fftoc_device_error_check.restype = c_int
     L.fftoc_auto_engine.argtypes = [c_int]
     L.fftoc_auto_engine.restype = c_int
     L.fftoc_status_string.argtypes = [c_int]
@@ -128,6 +133,8 @@ def _info_dict(info):
         "points_per_thread": info.points_per_thread,
         "variant": info.variant,
         "variants": info.variants,
+        "persistent": info.persistent,
+        "stages": info.stages,
     }
 
 

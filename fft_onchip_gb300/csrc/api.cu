@@ -96,6 +96,8 @@ struct DeviceState {
   std::string init_error;
   SizeVariants var[2][kNumSizes];                 // [engine: 0 f64, 1 fx][size]
   void* tw[2][kNumSizes][kMaxVariants] = {};      // per-variant twiddle tables
+  int* err = nullptr;                             // device error flag (bounded waits that gave up)
+  int sms = 0;
 };
 
 // Plan chosen per (engine, size): process-wide, set by fftoc_plan_select or
@@ -139,17 +141,32 @@ void build_twiddles(const KernelDesc& d, std::vector<double>& f64, std::vector<i
 void init_device(DeviceState& ds) {
   for (int eng = 0; eng < 2; ++eng)
     for (int i = 0; i < kNumSizes; ++i) ds.var[eng][i] = host_variants(eng)[i];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&ds.sms, cudaDevAttrMultiProcessorCount, dev);
+  {
+    cudaError_t e = cudaMalloc(&ds.err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(ds.err, 0, sizeof(int));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      ds.init_status = FFTOC_ERR_NO_MEMORY;
+      ds.init_error = std::string("cudaMalloc(error flag): ") + cudaGetErrorString(e);
+      return;
+    }
+  }
   for (int eng = 0; eng < 2; ++eng)
     for (int i = 0; i < kNumSizes; ++i)
       for (int v = 0; v < ds.var[eng][i].count; ++v) {
-        const KernelDesc& d = ds.var[eng][i].v[v];
+        KernelDesc& d = ds.var[eng][i].v[v];
         cudaError_t e = cudaFuncSetAttribute(d.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, d.smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.blocks_per_sm, d.fn, d.threads, d.smem);
         if (e != cudaSuccess) {
           cudaGetLastError();
           ds.init_status = FFTOC_ERR_CUDA;
-          ds.init_error = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
+          ds.init_error = std::string("kernel set-up: ") + cudaGetErrorString(e);
           return;
         }
+        if (d.blocks_per_sm < 1) d.blocks_per_sm = 1;
         std::vector<double> f64;
         std::vector<int> fx;
         build_twiddles(d, f64, fx);
@@ -234,12 +251,15 @@ fftoc_status launch_fwd(int n, const double* in, double* out, int64_t batch, int
   if (var >= ds->var[slot][idx].count) return fail(FFTOC_ERR_INVALID_VALUE, "no such plan variant");
   const KernelDesc& d = ds->var[slot][idx].v[var];
   const void* tw = ds->tw[slot][idx][var];
-  const long long blocks = (batch + d.tpb - 1) / d.tpb;
+  const long long tiles = (batch + d.tpb - 1) / d.tpb;
+  const long long cap = (long long)ds->sms * d.blocks_per_sm;
+  const long long blocks = d.persistent ? (tiles < cap ? tiles : cap) : tiles;
   if (blocks > 0x7FFFFFFFLL) return fail(FFTOC_ERR_INVALID_VALUE, "batch too large for one launch");
   const double2* in2 = reinterpret_cast<const double2*>(in);
   double2* out2 = reinterpret_cast<double2*>(out);
   long long bl = (long long)batch;
-  void* args[] = {(void*)&in2, (void*)&out2, (void*)&bl, (void*)&tw};
+  int* err = ds->err;
+  void* args[] = {(void*)&in2, (void*)&out2, (void*)&bl, (void*)&tw, (void*)&err};
   cudaError_t e = cudaLaunchKernel(d.fn, dim3((unsigned)blocks), dim3(d.threads), args, (size_t)d.smem, stream);
   if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchKernel");
   return FFTOC_OK;
@@ -318,6 +338,23 @@ fftoc_status plan_query(int n, int engine, int variant, fftoc_plan_info* info) {
   info->points_per_thread = d.ppt;
   info->variant = var;
   info->variants = sv.count;
+  info->persistent = d.persistent;
+  info->stages = d.stages;
+  return FFTOC_OK;
+}
+
+fftoc_status device_error_check() {
+  DeviceState* ds = nullptr;
+  fftoc_status st = device_state(&ds);
+  if (st != FFTOC_OK) return st;
+  int h = 0;
+  cudaError_t e = cudaMemcpy(&h, ds->err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(error flag)");
+  if (h != 0) {
+    e = cudaMemset(ds->err, 0, sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(error flag)");
+    return fail(FFTOC_ERR_TIMEOUT, "a kernel's bounded wait for its prefetched tile gave up");
+  }
   return FFTOC_OK;
 }
 
@@ -422,6 +459,8 @@ fftoc_status fftoc_plan_query_variant(int n, int engine, int variant, fftoc_plan
 }
 
 fftoc_status fftoc_plan_select(int n, int engine, int variant) { return fftoc::plan_select(n, engine, variant); }
+
+fftoc_status fftoc_device_error_check(void) { return fftoc::device_error_check(); }
 
 fftoc_status fftoc_autotune(int n, int engine, int64_t batch, fftoc_stream s, int* best_variant, float* best_ms) {
   return fftoc::autotune(n, engine, batch, (cudaStream_t)s, best_variant, best_ms);

@@ -25,9 +25,12 @@ struct KernelDesc {
   int passes = 0;
   int radix[4] = {1, 1, 1, 1};
   int tw_entries = 0;        // twiddle table entries (16 bytes each)
+  int persistent = 0;        // 1: grid-stride persistent CTAs with TMA prefetch (extra error-flag argument)
+  int stages = 0;            // shared-memory stages of the persistent kernel
+  int blocks_per_sm = 0;     // resident CTAs per SM (filled at device set-up)
 };
 
-constexpr int kMaxVariants = 4;
+constexpr int kMaxVariants = 6;
 struct SizeVariants {
   int count = 0;
   KernelDesc v[kMaxVariants];

@@ -1,5 +1,6 @@
 // fftoc — block fixed-point engine instantiations (every candidate plan per size).
 #include "fft_kernel.cuh"
+#include "fft_persistent.cuh"
 #include "internal.h"
 #include "plans.inc"
 

@@ -120,6 +120,8 @@ typedef struct {
   int points_per_thread;
   int variant;                /* index of this plan among the compiled ones  */
   int variants;               /* number of compiled plans for (n, engine)    */
+  int persistent;             /* 1: persistent CTAs, TMA-prefetched tiles    */
+  int stages;                 /* shared-memory stages (persistent plans)     */
 } fftoc_plan_info;
 
 /* Plan currently used for (n, engine). */
@@ -141,6 +143,12 @@ fftoc_status fftoc_plan_select(int n, int engine, int variant);
  * scripts/generate_bench.py:93-113 and src/saturation.cu:36-44.) */
 fftoc_status fftoc_autotune(int n, int engine, int64_t batch, fftoc_stream stream, int *best_variant,
                             float *best_ms);
+
+/* Device-side error flag of the current device: FFTOC_ERR_TIMEOUT if a
+ * persistent kernel's bounded wait for a prefetched tile gave up since the
+ * last check (its outputs are then incomplete), FFTOC_OK otherwise.  Clears
+ * the flag.  Synchronous. */
+fftoc_status fftoc_device_error_check(void);
 
 /* Engine that FFTOC_ENGINE_AUTO resolves to for size n. */
 int fftoc_auto_engine(int n);

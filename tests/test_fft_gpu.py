@@ -32,11 +32,17 @@ def run(torch, x, engine="auto", inplace=False):
 
 
 def per_transform_err(a, b):
-    # rows rescaled by their largest |b| first, so 1e300-sized values do not overflow
+    # rows rescaled exactly (by a power of two) so that 1e300-sized or
+    # subnormal values neither overflow nor underflow in the norm
     s = np.max(np.abs(b), axis=1, keepdims=True)
     s[s == 0] = 1.0
-    num = np.linalg.norm((a - b) / s, axis=1)
-    den = np.maximum(np.linalg.norm(b / s, axis=1), 1e-300)
+    k = -np.frexp(s)[1]
+
+    def sc(z):
+        return np.ldexp(z.real, k) + 1j * np.ldexp(z.imag, k)
+
+    num = np.linalg.norm(sc(a) - sc(b), axis=1)
+    den = np.maximum(np.linalg.norm(sc(b), axis=1), 1e-300)
     return num / den
 
 
