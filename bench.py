@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=1.5, help="CPU-baseline sample time per size")
     ap.add_argument("--gib", type=float, default=1.0, help="input GiB per size (1.0 = the sweep configuration)")
+    ap.add_argument("--plan", default="", help="N:variant,... plan overrides (default: the library's choice)")
+    ap.add_argument("--tuning", default="", help="tuning JSON written by fft_onchip_gb300.tune to apply")
     return ap.parse_args()
 
 
@@ -221,6 +223,11 @@ def run_reference(args, world, rank):
 # ----------------------------------------------------------------------------
 # GPU arm
 # ----------------------------------------------------------------------------
+def _plan_str(p):
+    return "%s%s P=%d tpb=%d" % ("persistent " if p.get("persistent") else "", "x".join(map(str, p["radix"])),
+                                 p["points_per_thread"], p["transforms_per_block"])
+
+
 def run_ours(args, world, rank, local):
     import torch
     import fft_onchip_gb300 as F
@@ -231,6 +238,12 @@ def run_ours(args, world, rank, local):
     L = F.load()
     sizes = [int(s) for s in args.sizes.split(",")]
     eng = F._engine_id(args.engine)
+    if args.tuning:
+        from fft_onchip_gb300 import tune as T
+        T.load(args.tuning)
+    for item in filter(None, args.plan.split(",")):
+        pn, pv = item.split(":")
+        F.plan_select(int(pn), eng if eng != F.ENGINE_AUTO else F.auto_engine(int(pn)), int(pv))
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
 
@@ -294,7 +307,8 @@ def run_ours(args, world, rank, local):
     traffic = tt.get(str(dom), {}).get(F.plan_query(dom, eng)["engine"] == F.ENGINE_FX and "fx" or "f64")
     roofline = {"bound": "hbm", "achieved": round(dom_gbs, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(dom_gbs / hbm, 4), "traffic": traffic,
-                "kernel": "fft_fwd_kernel N=%d (%s)" % (dom, "fx" if F.plan_query(dom, eng)["engine"] == F.ENGINE_FX else "f64"),
+                "kernel": "N=%d %s plan %s" % (dom, "fx" if F.plan_query(dom, eng)["engine"] == F.ENGINE_FX else "f64",
+                                               _plan_str(F.plan_query(dom, eng))),
                 "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured" else "fallback 6800 GB/s",
                 "algorithmic_bytes_per_launch": 32 * dom * bufs[dom][2]}
 
@@ -346,6 +360,7 @@ def run_ours(args, world, rank, local):
             "warmup": max(3, args.warmup), "ms_per_step": t_ms / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": dtype, "data": "synthetic",
             "config": {"workload": WORKLOAD, "sizes": sizes, "engine": args.engine,
+                       "plans": {str(n): _plan_str(F.plan_query(n, eng)) for n in sizes},
                        "bytes_per_step": sum(32 * n * bufs[n][2] for n in sizes),
                        "l2": "inputs and outputs (1 GiB each per size) larger than L2; no flush",
                        "parallelism": "replicas" if world > 1 else "single GPU"},

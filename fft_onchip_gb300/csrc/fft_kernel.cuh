@@ -86,6 +86,8 @@ template <int B>
 FFTOC_HD FxScale fx_scale(int em) {
   FxScale s;
   s.special = (em == 0x7FF);
+  // subnormals (exponent field 0) are scaled like exponent field 1
+  if (em < 1) em = 1;
   s.K = em - 1022 - B;
   s.kshift = (int)((unsigned)s.K << 20);
   s.slow = (em < B) || (em > 1983 + B);
