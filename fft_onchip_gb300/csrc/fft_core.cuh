@@ -68,6 +68,10 @@ struct EngF64 {
   static constexpr int kId = 1;
   FFTOC_HD static S add(S a, S b) { return a + b; }
   FFTOC_HD static S sub(S a, S b) { return a - b; }
+  FFTOC_HD static S add3(S a, S b, S c) { return (a + b) + c; }
+  FFTOC_HD static S addsub(S a, S b, S c) { return (a + b) - c; }
+  FFTOC_HD static S subadd(S a, S b, S c) { return (a - b) + c; }
+  FFTOC_HD static S sub3(S a, S b, S c) { return (a - b) - c; }
   FFTOC_HD static S mulc(S x, KC k) { return x * k.c; }
   FFTOC_HD static void cmul(S& xr, S& xi, const TW w) {
     const double r = fma(xr, w.x, -xi * w.y);
@@ -91,6 +95,35 @@ struct EngFx {
   static constexpr int kId = 2;
   FFTOC_HD static S add(S a, S b) { return a + b; }
   FFTOC_HD static S sub(S a, S b) { return a - b; }
+  // Three-operand sums as one PTX sequence each: the front end cannot share
+  // partial sums between outputs, so ptxas can emit a fused 3-input add pair.
+#ifdef __CUDA_ARCH__
+  FFTOC_HD static S add3(S a, S b, S c) {
+    S r;
+    asm("add.s64 %0, %1, %2;\n\tadd.s64 %0, %0, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+  }
+  FFTOC_HD static S addsub(S a, S b, S c) {
+    S r;
+    asm("add.s64 %0, %1, %2;\n\tsub.s64 %0, %0, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+  }
+  FFTOC_HD static S subadd(S a, S b, S c) {
+    S r;
+    asm("sub.s64 %0, %1, %2;\n\tadd.s64 %0, %0, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+  }
+  FFTOC_HD static S sub3(S a, S b, S c) {
+    S r;
+    asm("sub.s64 %0, %1, %2;\n\tsub.s64 %0, %0, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+  }
+#else
+  static S add3(S a, S b, S c) { return a + b + c; }
+  static S addsub(S a, S b, S c) { return a + b - c; }
+  static S subadd(S a, S b, S c) { return a - b + c; }
+  static S sub3(S a, S b, S c) { return a - b - c; }
+#endif
   // Limbs of a value, |x| < 2^61: x = xh*2^30 + xl, |xh| < 2^31, 0 <= xl < 2^30.
   FFTOC_HD static void split(S x, int& xh, int& xl) {
     xh = (int)(x >> 30);
@@ -155,22 +188,36 @@ FFTOC_HD void dft2(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
   re[B + ST] = E::sub(ar, br); im[B + ST] = E::sub(ai, bi);
 }
 
-template <class E, int B, int ST, int PP>
-FFTOC_HD void dft4(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
+// 4-point DFT of (x0, x1, x2, x3): with t = x1 + x3 and u = x1 - x3,
+//   y0 = x0 + x2 + t, y2 = x0 + x2 - t, y1 = x0 - x2 - i*u, y3 = x0 - x2 + i*u,
+// every output one three-operand sum.
+template <class E>
+FFTOC_HD void dft4_core(typename E::S x0r, typename E::S x0i, typename E::S x1r, typename E::S x1i,
+                        typename E::S x2r, typename E::S x2i, typename E::S x3r, typename E::S x3i,
+                        typename E::S& y0r, typename E::S& y0i, typename E::S& y1r, typename E::S& y1i,
+                        typename E::S& y2r, typename E::S& y2i, typename E::S& y3r, typename E::S& y3i) {
   using S = typename E::S;
-  const S s0r = E::add(re[B], re[B + 2 * ST]), s0i = E::add(im[B], im[B + 2 * ST]);
-  const S d0r = E::sub(re[B], re[B + 2 * ST]), d0i = E::sub(im[B], im[B + 2 * ST]);
-  const S s1r = E::add(re[B + ST], re[B + 3 * ST]), s1i = E::add(im[B + ST], im[B + 3 * ST]);
-  const S d1r = E::sub(re[B + ST], re[B + 3 * ST]), d1i = E::sub(im[B + ST], im[B + 3 * ST]);
-  re[B] = E::add(s0r, s1r); im[B] = E::add(s0i, s1i);
-  re[B + 2 * ST] = E::sub(s0r, s1r); im[B + 2 * ST] = E::sub(s0i, s1i);
-  // y1 = d0 - i*d1, y3 = d0 + i*d1
-  re[B + ST] = E::add(d0r, d1i); im[B + ST] = E::sub(d0i, d1r);
-  re[B + 3 * ST] = E::sub(d0r, d1i); im[B + 3 * ST] = E::add(d0i, d1r);
+  const S tr = E::add(x1r, x3r), ti = E::add(x1i, x3i);
+  const S ur = E::sub(x1r, x3r), ui = E::sub(x1i, x3i);
+  y0r = E::add3(x0r, x2r, tr);
+  y0i = E::add3(x0i, x2i, ti);
+  y2r = E::addsub(x0r, x2r, tr);
+  y2i = E::addsub(x0i, x2i, ti);
+  y1r = E::subadd(x0r, x2r, ui);
+  y1i = E::sub3(x0i, x2i, ur);
+  y3r = E::sub3(x0r, x2r, ui);
+  y3i = E::subadd(x0i, x2i, ur);
 }
 
-// 8-point DFT: radix-2 split into two 4-point DFTs; W8^1, W8^3 as real
-// constant products (sqrt(1/2)).
+template <class E, int B, int ST, int PP>
+FFTOC_HD void dft4(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
+  dft4_core<E>(re[B], im[B], re[B + ST], im[B + ST], re[B + 2 * ST], im[B + 2 * ST], re[B + 3 * ST], im[B + 3 * ST],
+               re[B], im[B], re[B + ST], im[B + ST], re[B + 2 * ST], im[B + 2 * ST], re[B + 3 * ST], im[B + 3 * ST]);
+}
+
+// 8-point DFT: a_m = x_m + x_{m+4}, b_m = (x_m - x_{m+4}) W8^m; even outputs
+// are DFT4(a), odd outputs DFT4(b).  W8^1 and W8^3 are real-constant
+// products (sqrt(1/2)); W8^2 = -i is folded into the odd DFT4's signs.
 template <class E, int B, int ST, int PP>
 FFTOC_HD void dft8(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
   using S = typename E::S;
@@ -183,39 +230,26 @@ FFTOC_HD void dft8(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
     br[m] = E::sub(re[B + m * ST], re[B + (m + 4) * ST]);
     bi[m] = E::sub(im[B + m * ST], im[B + (m + 4) * ST]);
   }
-  // b1 *= (1 - i)/sqrt2 ; b2 *= -i ; b3 *= (-1 - i)/sqrt2
+  // b1 *= (1 - i)/sqrt2 ; b3 *= (-1 - i)/sqrt2
+  const S b1r = E::mulc(E::add(br[1], bi[1]), K::h());
+  const S b1i = E::mulc(E::sub(bi[1], br[1]), K::h());
+  const S b3r = E::mulc(E::sub(bi[3], br[3]), K::h());
+  const S b3i = E::mulc(E::add(br[3], bi[3]), K::nh());
+  // even outputs X0, X2, X4, X6
+  dft4_core<E>(ar[0], ai[0], ar[1], ai[1], ar[2], ai[2], ar[3], ai[3], re[B], im[B], re[B + 2 * ST], im[B + 2 * ST],
+               re[B + 4 * ST], im[B + 4 * ST], re[B + 6 * ST], im[B + 6 * ST]);
+  // odd outputs X1, X3, X5, X7: DFT4(b0, b1', b2', b3') with b2' = -i*b2 = (b2i, -b2r)
   {
-    const S r = E::mulc(E::add(br[1], bi[1]), K::h());
-    const S i = E::mulc(E::sub(bi[1], br[1]), K::h());
-    br[1] = r; bi[1] = i;
-    const S r2 = bi[2], i2 = br[2];  // (-i)*(x+iy) = y - i x : im becomes -br[2]
-    br[2] = r2; bi[2] = i2;           // bi[2] holds +br[2]; sign folded below
-    const S r3 = E::mulc(E::sub(bi[3], br[3]), K::h());
-    const S i3 = E::mulc(E::add(br[3], bi[3]), K::nh());
-    br[3] = r3; bi[3] = i3;
-  }
-  // even outputs: DFT4(a)
-  {
-    const S s0r = E::add(ar[0], ar[2]), s0i = E::add(ai[0], ai[2]);
-    const S d0r = E::sub(ar[0], ar[2]), d0i = E::sub(ai[0], ai[2]);
-    const S s1r = E::add(ar[1], ar[3]), s1i = E::add(ai[1], ai[3]);
-    const S d1r = E::sub(ar[1], ar[3]), d1i = E::sub(ai[1], ai[3]);
-    re[B] = E::add(s0r, s1r); im[B] = E::add(s0i, s1i);
-    re[B + 4 * ST] = E::sub(s0r, s1r); im[B + 4 * ST] = E::sub(s0i, s1i);
-    re[B + 2 * ST] = E::add(d0r, d1i); im[B + 2 * ST] = E::sub(d0i, d1r);
-    re[B + 6 * ST] = E::sub(d0r, d1i); im[B + 6 * ST] = E::add(d0i, d1r);
-  }
-  // odd outputs: DFT4(b0, b1', b2', b3'), with b2' = (bi2, -br2) stored as (br[2], bi[2]) = (bi2, br2)
-  {
-    // b2' real = br[2], b2' imag = -bi[2]
-    const S s0r = E::add(br[0], br[2]), s0i = E::sub(bi[0], bi[2]);
-    const S d0r = E::sub(br[0], br[2]), d0i = E::add(bi[0], bi[2]);
-    const S s1r = E::add(br[1], br[3]), s1i = E::add(bi[1], bi[3]);
-    const S d1r = E::sub(br[1], br[3]), d1i = E::sub(bi[1], bi[3]);
-    re[B + ST] = E::add(s0r, s1r); im[B + ST] = E::add(s0i, s1i);
-    re[B + 5 * ST] = E::sub(s0r, s1r); im[B + 5 * ST] = E::sub(s0i, s1i);
-    re[B + 3 * ST] = E::add(d0r, d1i); im[B + 3 * ST] = E::sub(d0i, d1r);
-    re[B + 7 * ST] = E::sub(d0r, d1i); im[B + 7 * ST] = E::add(d0i, d1r);
+    const S tr = E::add(b1r, b3r), ti = E::add(b1i, b3i);
+    const S ur = E::sub(b1r, b3r), ui = E::sub(b1i, b3i);
+    re[B + ST] = E::add3(br[0], bi[2], tr);
+    im[B + ST] = E::subadd(bi[0], br[2], ti);
+    re[B + 5 * ST] = E::addsub(br[0], bi[2], tr);
+    im[B + 5 * ST] = E::sub3(bi[0], br[2], ti);
+    re[B + 3 * ST] = E::subadd(br[0], bi[2], ui);
+    im[B + 3 * ST] = E::addsub(bi[0], br[2], ur);
+    re[B + 7 * ST] = E::sub3(br[0], bi[2], ui);
+    im[B + 7 * ST] = E::add3(bi[0], br[2], ur);
   }
 }
 

@@ -95,6 +95,48 @@ FFTOC_HD FxScale fx_scale(int em) {
   return s;
 }
 
+// Fast conversion for values within 2^31 of the transform's largest exponent
+// (all normal): (mantissa | implicit bit) >> d with d < 32 needs two funnel
+// shifts.  Bit-identical to fx_in for those values.
+FFTOC_HD long long fx_in_near(unsigned hw, unsigned lw, int eref) {
+  const int d = eref - expo_of(hw);
+  const unsigned mh = (hw & 0xFFFFFu) | 0x100000u;
+#ifdef __CUDA_ARCH__
+  const unsigned lo = __funnelshift_r(lw, mh, d);
+#else
+  const unsigned lo = (unsigned)((((unsigned long long)mh << 32) | lw) >> d);
+#endif
+  const unsigned hi = mh >> d;
+  const long long m = (long long)(((unsigned long long)hi << 32) | lo);
+  return ((int)hw < 0) ? -m : m;
+}
+
+// Convert a thread's P raw points; the fast path is taken when every value is
+// normal and within 2^31 of the transform maximum (the usual case).
+template <int P>
+FFTOC_HD void fx_convert_in(const double2 (&raw)[P], long long (&re)[P], long long (&im)[P], int eref) {
+  int emin = 0x7FF;
+#pragma unroll
+  for (int i = 0; i < P; ++i) {
+    const int a = expo_of(hi_word(raw[i].x)), b = expo_of(hi_word(raw[i].y));
+    emin = emin < a ? emin : a;
+    emin = emin < b ? emin : b;
+  }
+  if (emin >= 1 && eref - emin < 32) {
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      re[i] = fx_in_near(hi_word(raw[i].x), lo_word(raw[i].x), eref);
+      im[i] = fx_in_near(hi_word(raw[i].y), lo_word(raw[i].y), eref);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      re[i] = fx_in(hi_word(raw[i].x), lo_word(raw[i].x), eref);
+      im[i] = fx_in(hi_word(raw[i].y), lo_word(raw[i].y), eref);
+    }
+  }
+}
+
 // --- the kernel ---------------------------------------------------------------
 template <class E, class PL>
 struct Fft {
@@ -105,15 +147,17 @@ struct Fft {
   static constexpr int P = PL::P;
   static constexpr int T = PL::T;
   static constexpr int NS = PL::S;
-  static constexpr int SW = ilog2c(PL::R[0]) < 3 ? 3 : ilog2c(PL::R[0]);
+  // padded shared layout: one 16-byte pad slot after every 2^SH points, so
+  // the first pass's stride-R writes and every stride-1 read hit distinct
+  // bank groups, and all addresses are a per-thread base plus a constant
+  static constexpr int SH = PL::R[0] >= 16 ? 4 : 3;
+  static constexpr int NP = N + (N >> SH);
   static constexpr int THREADS = T * TPB;
   static constexpr bool STAGED = T < 8;  // small N: stage HBM tiles through smem
-  static constexpr int SMEM = TPB * N * 16 + 64;
+  static constexpr int SMEM = TPB * NP * 16 + 64;
 
   // 16-byte slot of element e of block-local transform j
-  __device__ __forceinline__ static int slot(int j, int e) {
-    return j * N + (e ^ (((e >> SW) ^ (j * T)) & 7));
-  }
+  __device__ __forceinline__ static int slot(int j, int e) { return j * NP + e + (e >> SH); }
 
   template <int s, int b>
   __device__ __forceinline__ static void butterfly(S (&re)[P], S (&im)[P], int t, const TW* __restrict__ tw) {
@@ -258,7 +302,7 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
       // warps of one transform are contiguous: reduce per warp, then in smem
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
-      int* red = reinterpret_cast<int*>(smem_raw + TPB * N * 16);
+      int* red = reinterpret_cast<int*>(smem_raw + TPB * F::NP * 16);
       if (tid < TPB) red[tid] = 0;
       __syncthreads();
       if ((tid & 31) == 0) atomicMax(&red[j], em);
@@ -270,12 +314,7 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
     K = sc.K;
     kshift = sc.kshift;
     slow = sc.slow;
-    const int eref = sc.eref;
-#pragma unroll
-    for (int i = 0; i < P; ++i) {
-      re[i] = fx_in(hi_word(raw[i].x), lo_word(raw[i].x), eref);
-      im[i] = fx_in(hi_word(raw[i].y), lo_word(raw[i].y), eref);
-    }
+    fx_convert_in<P>(raw, re, im, sc.eref);
   }
 
   if constexpr (F::STAGED) __syncthreads();  // staging buffer is reused by the passes

@@ -62,10 +62,11 @@ template <class E, class PL, int NSTAGE>
 struct Persist {
   using F = Fft<E, PL>;
   static constexpr int N = PL::N, TPB = PL::TPB, P = PL::P, T = PL::T, NS = PL::S;
-  static constexpr int TILE_BYTES = TPB * N * 16;
+  static constexpr int TILE_BYTES = TPB * N * 16;                           // bytes loaded per tile
+  static constexpr int STAGE_BYTES = ((TPB * F::NP * 16 + 127) / 128) * 128;  // padded exchange layout
   static constexpr int THREADS = F::THREADS;
   // stages, then TPB ints of exponent scratch, then NSTAGE mbarriers
-  static constexpr int RED_OFF = NSTAGE * TILE_BYTES;
+  static constexpr int RED_OFF = NSTAGE * STAGE_BYTES;
   static constexpr int BAR_OFF = RED_OFF + 64;
   static constexpr int SMEM = BAR_OFF + 8 * NSTAGE;
   static_assert(T >= 8, "pass-0 reads of the linear tile need >= 8 threads per transform");
@@ -101,7 +102,7 @@ fft_fwd_persistent(const double2* __restrict__ in, double2* __restrict__ out, lo
     const long long cnt = min((long long)TPB, batch - t0);
     const unsigned bytes = (unsigned)(cnt * N * 16);
     mbar_expect_tx(&bars[s], bytes);
-    bulk_load(smem_raw + s * C::TILE_BYTES, in + t0 * N, bytes, &bars[s]);
+    bulk_load(smem_raw + s * C::STAGE_BYTES, in + t0 * N, bytes, &bars[s]);
   };
 
   // prologue: the first NSTAGE-1 tiles of this CTA
@@ -135,7 +136,7 @@ fft_fwd_persistent(const double2* __restrict__ in, double2* __restrict__ out, lo
       return;
     }
 
-    longlong2* sm = reinterpret_cast<longlong2*>(smem_raw + s * C::TILE_BYTES);
+    longlong2* sm = reinterpret_cast<longlong2*>(smem_raw + s * C::STAGE_BYTES);
     const long long tr = tile * TPB + j;
     const bool active = tr < batch;
 
@@ -151,16 +152,13 @@ fft_fwd_persistent(const double2* __restrict__ in, double2* __restrict__ out, lo
         im[i] = __longlong_as_double(v.y);
       }
     } else {
-      unsigned hw[2 * P], lw[2 * P];
+      double2 raw[P];
       int em = 0;
 #pragma unroll
       for (int i = 0; i < P; ++i) {
         const longlong2 v = active ? sm[j * N + t + T * i] : make_longlong2(0, 0);
-        hw[2 * i] = (unsigned)((unsigned long long)v.x >> 32);
-        lw[2 * i] = (unsigned)v.x;
-        hw[2 * i + 1] = (unsigned)((unsigned long long)v.y >> 32);
-        lw[2 * i + 1] = (unsigned)v.y;
-        em = max(em, max(expo_of(hw[2 * i]), expo_of(hw[2 * i + 1])));
+        raw[i] = make_double2(__longlong_as_double(v.x), __longlong_as_double(v.y));
+        em = max(em, max(expo_of(hi_word(raw[i].x)), expo_of(hi_word(raw[i].y))));
       }
       if constexpr (T <= 32) {
 #pragma unroll
@@ -179,11 +177,7 @@ fft_fwd_persistent(const double2* __restrict__ in, double2* __restrict__ out, lo
       K = sc.K;
       kshift = sc.kshift;
       slow = sc.slow;
-#pragma unroll
-      for (int i = 0; i < P; ++i) {
-        re[i] = fx_in(hw[2 * i], lw[2 * i], sc.eref);
-        im[i] = fx_in(hw[2 * i + 1], lw[2 * i + 1], sc.eref);
-      }
+      fx_convert_in<P>(raw, re, im, sc.eref);
     }
     if constexpr (NS > 1) __syncthreads();  // every linear read is done before pass-0 writes
     F::template run_passes<0>(re, im, j, t, tw, sm);
