@@ -129,14 +129,25 @@ struct EngFx {
     xh = (int)(x >> 30);
     xl = (int)((unsigned)x & 0x3FFFFFFFu);
   }
+  // a*b + c with a, b 32-bit and c 64-bit: one IMAD.WIDE (spelled out in PTX;
+  // written as (long long)a * b + c the front end may emit a 64x64 multiply)
+  FFTOC_HD static S madw(int a, int b, S c) {
+#ifdef __CUDA_ARCH__
+    S d;
+    asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+    return d;
+#else
+    return (S)a * (S)b + c;
+#endif
+  }
   // x * c for a real constant, |c| <= 1:
   //   x*c = xh*ch + (xh*cl + xl*ch) / 2^30 + xl*cl/2^60   (last term < 1, dropped)
   // |xh*cl| < 2^61, |xl*ch| <= 2^60, so the middle sum cannot overflow.
   FFTOC_HD static S mulc(S x, KC k) {
     int xh, xl;
     split(x, xh, xl);
-    const long long m = (long long)xh * k.l + (long long)xl * k.h + (1LL << 29);
-    return (long long)xh * k.h + (m >> 30);
+    const long long m = madw(xl, k.h, madw(xh, k.l, 1LL << 29));
+    return madw(xh, k.h, m >> 30);
   }
   // (xr + i xi) * (wr + i wi); each middle sum has four terms of magnitude
   // < 2^61 or <= 2^60, so |m| < 1.5 * 2^62.
@@ -144,12 +155,13 @@ struct EngFx {
     int rh, rl, ih, il;
     split(xr, rh, rl);
     split(xi, ih, il);
-    const long long mr = (long long)rh * wrl + (long long)rl * wrh - (long long)ih * wil - (long long)il * wih +
-                         (1LL << 29);
-    const long long mi = (long long)rh * wil + (long long)rl * wih + (long long)ih * wrl + (long long)il * wrh +
-                         (1LL << 29);
-    xr = (long long)rh * wrh - (long long)ih * wih + (mr >> 30);
-    xi = (long long)rh * wih + (long long)ih * wrh + (mi >> 30);
+    // negate the twiddle limbs (|wih| <= 2^30, 0 <= wil < 2^30), never the
+    // data limbs (ih may be -2^31)
+    const int nwih = -wih, nwil = -wil;
+    const long long mr = madw(il, nwih, madw(ih, nwil, madw(rl, wrh, madw(rh, wrl, 1LL << 29))));
+    const long long mi = madw(il, wrh, madw(ih, wrl, madw(rl, wih, madw(rh, wil, 1LL << 29))));
+    xr = madw(ih, nwih, madw(rh, wrh, mr >> 30));
+    xi = madw(ih, wrh, madw(rh, wih, mi >> 30));
   }
   FFTOC_HD static void cmul(S& xr, S& xi, const int4 w) { cmul_limbs(xr, xi, w.x, w.y, w.z, w.w); }
   FFTOC_HD static void cmulk(S& xr, S& xi, KC c, KC s) { cmul_limbs(xr, xi, c.h, c.l, s.h, s.l); }
