@@ -32,11 +32,12 @@ namespace fftoc {
 // ---------------------------------------------------------------------------
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
-template <int N_, int P_, int TPB_, int R0, int R1 = 1, int R2 = 1, int R3 = 1>
+template <int N_, int P_, int TPB_, int R0, int R1 = 1, int R2 = 1, int R3 = 1, int MINB_ = 1>
 struct PlanT {
   static constexpr int N = N_;
   static constexpr int P = P_;
   static constexpr int TPB = TPB_;
+  static constexpr int MINB = MINB_;  // minimum resident CTAs per SM (register budget)
   static constexpr int R[4] = {R0, R1, R2, R3};
   static constexpr int S = (R0 > 1) + (R1 > 1) + (R2 > 1) + (R3 > 1);
   static constexpr int T = N / P;

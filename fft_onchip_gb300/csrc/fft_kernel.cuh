@@ -243,7 +243,7 @@ struct Fft {
 // Engine-specific entry/exit: load raw points (binary64), convert, run the
 // passes, convert back and store.
 template <class E, class PL>
-__global__ void __launch_bounds__(Fft<E, PL>::THREADS)
+__global__ void __launch_bounds__(Fft<E, PL>::THREADS, PL::MINB)
 fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long long batch,
                const typename E::TW* __restrict__ tw, int* __restrict__ err) {
   (void)err;  // no waits in this kernel; the argument keeps one launch signature

@@ -74,7 +74,7 @@ struct Persist {
 };
 
 template <class E, class PL, int NSTAGE>
-__global__ void __launch_bounds__(Fft<E, PL>::THREADS)
+__global__ void __launch_bounds__(Fft<E, PL>::THREADS, PL::MINB)
 fft_fwd_persistent(const double2* __restrict__ in, double2* __restrict__ out, long long batch,
                    const typename E::TW* __restrict__ tw, int* __restrict__ err) {
   using F = Fft<E, PL>;

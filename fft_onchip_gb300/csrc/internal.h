@@ -30,7 +30,7 @@ struct KernelDesc {
   int blocks_per_sm = 0;     // resident CTAs per SM (filled at device set-up)
 };
 
-constexpr int kMaxVariants = 6;
+constexpr int kMaxVariants = 8;
 struct SizeVariants {
   int count = 0;
   KernelDesc v[kMaxVariants];
