@@ -19,7 +19,7 @@ from . import _lib
 SIZES = _lib.SIZES
 
 
-def time_variants(n, engine, gib=0.5, reps=5, warmup=3, device=0):
+def time_variants(n, engine, gib=0.5, reps=20, warmup=5, device=0, rounds=2):
     """[(variant, ms per launch, plan dict)] for every compiled plan."""
     import torch
     torch.cuda.set_device(device)
@@ -36,13 +36,16 @@ def time_variants(n, engine, gib=0.5, reps=5, warmup=3, device=0):
             _lib.plan_select(n, eid, v)
             for _ in range(warmup):
                 _lib.check(L.fftoc_c2c_fwd_ex(n, x.data_ptr(), y.data_ptr(), batch, eid, s.cuda_stream))
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(s)
-            for _ in range(reps):
-                _lib.check(L.fftoc_c2c_fwd_ex(n, x.data_ptr(), y.data_ptr(), batch, eid, s.cuda_stream))
-            b.record(s)
-            b.synchronize()
-            out.append((v, a.elapsed_time(b) / reps, _lib.plan_query(n, eid, variant=v)))
+            best = float("inf")
+            for _ in range(rounds):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(s)
+                for _ in range(reps):
+                    _lib.check(L.fftoc_c2c_fwd_ex(n, x.data_ptr(), y.data_ptr(), batch, eid, s.cuda_stream))
+                b.record(s)
+                b.synchronize()
+                best = min(best, a.elapsed_time(b) / reps)
+            out.append((v, best, _lib.plan_query(n, eid, variant=v)))
     finally:
         _lib.plan_select(n, eid, cur["variant"])
     return out
