@@ -95,7 +95,7 @@ def fixtures():
     from fft_onchip_gb300 import inputs
     drv = Driver()
     for name, (n, threads, staged) in EXECUTORS.items():
-        batch = 64 if n <= 512 else 8
+        batch = 16 if n <= 64 else (4 if n <= 512 else 1)
         x = inputs.uniform(n, batch, seed=7)
         y = run(drv, name, x)
         np.savez_compressed(os.path.join(GOLD, "ref_out_%s.npz" % name[4:]), x=x, y=y)
