@@ -31,6 +31,7 @@ EXPORTS = tuple(["fftoc_c2c_fwd_n%d" % n for n in SIZES]) + (
     "fftoc_c2c_fwd",
     "fftoc_c2c_fwd_ex",
     "fftoc_c2c_fwd_host",
+    "fftoc_c2c_fwd_host_noalloc",
     "fftoc_plan_query",
     "fftoc_plan_query_variant",
     "fftoc_plan_select",
@@ -91,6 +92,8 @@ def load(path=None):
     L.fftoc_c2c_fwd_ex.restype = c_int
     L.fftoc_c2c_fwd_host.argtypes = [c_int, vp, vp, i64, c_int, vp]
     L.fftoc_c2c_fwd_host.restype = c_int
+    L.fftoc_c2c_fwd_host_noalloc.argtypes = [c_int, vp, vp, i64, c_int, vp]
+    L.fftoc_c2c_fwd_host_noalloc.restype = c_int
     L.fftoc_plan_query.argtypes = [c_int, c_int, ctypes.POINTER(PlanInfo)]
     L.fftoc_plan_query.restype = c_int
     L.fftoc_plan_query_variant.argtypes = [c_int, c_int, c_int, ctypes.POINTER(PlanInfo)]

@@ -227,6 +227,13 @@ int resolve_engine(int n, int engine) {
 
 }  // namespace
 
+// Accessors for other translation units (the allocation-free entry point).
+const SizeVariants* compiled_variants(int eng_slot) { return host_variants(eng_slot); }
+void twiddle_tables(const KernelDesc& d, std::vector<double>& f64, std::vector<int>& fx) { build_twiddles(d, f64, fx); }
+int chosen_variant(int eng_slot, int idx) { return g_choice[eng_slot][idx].load(std::memory_order_relaxed); }
+int resolved_engine(int n, int engine) { return resolve_engine(n, engine); }
+fftoc_status set_error(fftoc_status st, const std::string& msg) { return fail(st, msg); }
+
 fftoc_status launch_fwd(int n, const double* in, double* out, int64_t batch, int engine, cudaStream_t stream,
                         int variant = -1) {
   const int idx = size_index(n);

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <string>
+#include <vector>
 
 namespace fftoc {
 
@@ -40,5 +42,14 @@ struct SizeVariants {
 // (kernels_<engine>.cu); variant 0 is the default choice.
 void describe_f64(SizeVariants* per_size);
 void describe_fx(SizeVariants* per_size);
+
+// api.cu accessors: compiled plans per engine slot (0 F64, 1 FX), twiddle
+// tables of a plan (16 bytes per entry: double2 / 4 x int32 limbs), the plan
+// currently chosen for (slot, size index), AUTO resolution, and the
+// per-thread error message.
+const SizeVariants* compiled_variants(int eng_slot);
+void twiddle_tables(const KernelDesc& d, std::vector<double>& f64, std::vector<int>& fx);
+int chosen_variant(int eng_slot, int idx);
+int resolved_engine(int n, int engine);
 
 }  // namespace fftoc

@@ -106,6 +106,23 @@ fftoc_status fftoc_c2c_fwd_ex(int n, const double *in, double *out, int64_t batc
 fftoc_status fftoc_c2c_fwd_host(int n, const double *h_in, double *h_out, int64_t batch, int engine,
                                 fftoc_stream stream);
 
+/* Host buffers in and out, with no device allocation (no counterpart in the
+ * reference).  For callers that cannot let a library call cudaMalloc: device
+ * memory already claimed by another allocator or a fixed pool, services that
+ * must not grow their device footprint after start-up, code that cannot take
+ * cudaMalloc's implicit synchronisation.  The batch is staged in a 32 MiB
+ * array compiled into the library (file-scope __device__ memory that every
+ * GPU loading the library holds until exit): batch*n*16 must be at most
+ * 32 MiB, larger batches are rejected with FFTOC_ERR_INVALID_VALUE.  H2D
+ * copy, transform (the plan fftoc_plan_query reports) and D2H copy run on
+ * `stream`; synchronise it before reading h_out.  All calls share that one
+ * array: calls that overlap on the GPU (other streams, other host threads)
+ * race and corrupt each other's results — serialise them.  The first call on
+ * a device does the set-up (array addresses, twiddle upload into another
+ * compiled-in array, kernel attributes): make it before any stream capture. */
+fftoc_status fftoc_c2c_fwd_host_noalloc(int n, const double *h_in, double *h_out, int64_t batch, int engine,
+                                        fftoc_stream stream);
+
 /* Launch geometry of a size/engine (reference: the FFTExec static members
  * threads / units_per_block / ffts_per_unit, e.g. tensor_fft_64.cuh:16-19). */
 typedef struct {
