@@ -126,28 +126,9 @@ struct EngFx {
   static S sub3(S a, S b, S c) { return a - b - c; }
 #endif
   // Limbs of a value, |x| < 2^61: x = xh*2^30 + xl, |xh| < 2^31, 0 <= xl < 2^30.
-  // xh is one funnel shift (ALU pipe); xl = lo - xh*2^30 is one IMAD (FMA
-  // pipe), which keeps the integer ALU pipe, the bottleneck, free.
   FFTOC_HD static void split(S x, int& xh, int& xl) {
     xh = (int)(x >> 30);
-#ifdef __CUDA_ARCH__
-    asm("mad.lo.s32 %0, %1, -1073741824, %2;" : "=r"(xl) : "r"(xh), "r"((int)x));
-#else
     xl = (int)((unsigned)x & 0x3FFFFFFFu);
-#endif
-  }
-  // m >> 30 for the middle sums: low word by a funnel shift, high word by
-  // mul.hi(m_hi, 4) on the FMA pipe.
-  FFTOC_HD static S shr30(S m) {
-#ifdef __CUDA_ARCH__
-    const int mhi = (int)(m >> 32);
-    int hi;
-    asm("mul.hi.s32 %0, %1, 4;" : "=r"(hi) : "r"(mhi));
-    const unsigned lo = __funnelshift_r((unsigned)m, (unsigned)mhi, 30);
-    return (S)(((unsigned long long)(unsigned)hi << 32) | lo);
-#else
-    return m >> 30;
-#endif
   }
   // a*b + c with a, b 32-bit and c 64-bit: one IMAD.WIDE (spelled out in PTX;
   // written as (long long)a * b + c the front end may emit a 64x64 multiply)
@@ -167,7 +148,7 @@ struct EngFx {
     int xh, xl;
     split(x, xh, xl);
     const long long m = madw(xl, k.h, madw(xh, k.l, 1LL << 29));
-    return madw(xh, k.h, shr30(m));
+    return madw(xh, k.h, m >> 30);
   }
   // (xr + i xi) * (wr + i wi); each middle sum has four terms of magnitude
   // < 2^61 or <= 2^60, so |m| < 1.5 * 2^62.
@@ -180,8 +161,8 @@ struct EngFx {
     const int nwih = -wih, nwil = -wil;
     const long long mr = madw(il, nwih, madw(ih, nwil, madw(rl, wrh, madw(rh, wrl, 1LL << 29))));
     const long long mi = madw(il, wrh, madw(ih, wrl, madw(rl, wih, madw(rh, wil, 1LL << 29))));
-    xr = madw(ih, nwih, madw(rh, wrh, shr30(mr)));
-    xi = madw(ih, wrh, madw(rh, wih, shr30(mi)));
+    xr = madw(ih, nwih, madw(rh, wrh, mr >> 30));
+    xi = madw(ih, wrh, madw(rh, wih, mi >> 30));
   }
   FFTOC_HD static void cmul(S& xr, S& xi, const int4 w) { cmul_limbs(xr, xi, w.x, w.y, w.z, w.w); }
   FFTOC_HD static void cmulk(S& xr, S& xi, KC c, KC s) { cmul_limbs(xr, xi, c.h, c.l, s.h, s.l); }

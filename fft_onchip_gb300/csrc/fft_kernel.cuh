@@ -123,19 +123,9 @@ FFTOC_HD void fx_convert_in(const double2 (&raw)[P], long long (&re)[P], long lo
     emin = emin < b ? emin : b;
   }
   if (emin >= 1 && eref - emin < 32) {
-    // value * 2^(1075 - eref): every exponent here is in [eref - 31, eref], so
-    // the exponent add stays in the normal range and the truncating
-    // conversion (FP64 pipe) is bit-identical to fx_in_near (ALU pipe); the
-    // real parts take that route, the imaginary parts the integer one.
-    const unsigned kadd = (unsigned)(1075 - eref) << 20;
 #pragma unroll
     for (int i = 0; i < P; ++i) {
-#ifdef __CUDA_ARCH__
-      re[i] = __double2ll_rz(from_words(hi_word(raw[i].x) + kadd, lo_word(raw[i].x)));
-#else
       re[i] = fx_in_near(hi_word(raw[i].x), lo_word(raw[i].x), eref);
-      (void)kadd;
-#endif
       im[i] = fx_in_near(hi_word(raw[i].y), lo_word(raw[i].y), eref);
     }
   } else {
