@@ -303,8 +303,13 @@ def run_ours(args, world, rank, local):
                          "hbm_gbs": round(gbs, 1), "frac_hbm": round(gbs / hbm, 4)}
     dom = max(sizes, key=lambda n: launch_ms[n])
     dom_gbs = 32.0 * dom * bufs[dom][2] / (launch_ms[dom] * 1e-3) / 1e9
-    tt = traffic_table()
-    traffic = tt.get(str(dom), {}).get(F.plan_query(dom, eng)["engine"] == F.ENGINE_FX and "fx" or "f64")
+    # per-launch DRAM bytes from the committed capture, used only when it was
+    # taken on the plan that ran here
+    tt = traffic_table().get(str(dom), {})
+    dom_plan = F.plan_query(dom, eng)
+    traffic = tt.get("fx" if dom_plan["engine"] == F.ENGINE_FX else "f64")
+    if tt.get("plan") != _plan_str(dom_plan):
+        traffic = None
     roofline = {"bound": "hbm", "achieved": round(dom_gbs, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(dom_gbs / hbm, 4), "traffic": traffic,
                 "kernel": "N=%d %s plan %s" % (dom, "fx" if F.plan_query(dom, eng)["engine"] == F.ENGINE_FX else "f64",
