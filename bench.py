@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--gib", type=float, default=1.0, help="input GiB per size (1.0 = the sweep configuration)")
     ap.add_argument("--plan", default="", help="N:variant,... plan overrides (default: the library's choice)")
     ap.add_argument("--tuning", default="", help="tuning JSON written by fft_onchip_gb300.tune to apply")
+    ap.add_argument("--forms", default="uneven",
+                    help="extra workloads measured after the sweep (comma list of: uneven; empty for none)")
+    ap.add_argument("--uneven-count", type=int, default=200000)
     return ap.parse_args()
 
 
@@ -349,6 +352,10 @@ def run_ours(args, world, rank, local):
                "steps": E, "ms_per_step": 1e3 * el / E, "path": "fftoc_c2c_fwd_host (pinned, 64 MiB chunks)"}
         del h_in, h_out
 
+    forms = {}
+    if "uneven" in args.forms.split(","):
+        forms["uneven"] = bench_uneven(args, torch, F, dev, stream, world)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         v, cores, per = cpu_sample_rate(sizes, args.cpu_seconds)
@@ -371,8 +378,54 @@ def run_ours(args, world, rank, local):
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "per_n": per_n, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": K * len(sizes), "clocks": clocks, "max_rel_err_vs_oracle": max_err,
+            "forms": forms,
         }
         print(json.dumps(line), flush=True)
+
+
+def bench_uneven(args, torch, F, dev, stream, world):
+    """Mixed-size batch: `count` transforms, N in 8..4096 with P ~ 1/log2 N,
+    packed back to back with an int64 offset table, re/im uniform [-1, 1).
+    One CUDA graph per batch (device bucketing + one persistent kernel per
+    size) against one launch per size after a host read of the counts."""
+    from fft_onchip_gb300 import inputs
+    count = args.uneven_count
+    ns = inputs.uneven_sizes(count, seed=0)
+    off, total = inputs.uneven_layout(ns)
+    g = torch.Generator(device=dev).manual_seed(4)
+    x = torch.view_as_complex(torch.rand(total, 2, dtype=torch.float64, device=dev, generator=g) * 2 - 1)
+    y = torch.empty_like(x)
+    d_off = torch.from_numpy(off).to(dev)
+    d_ns = torch.from_numpy(ns).to(dev)
+    plan = F.UnevenPlan(count)
+    algo_bytes = 32 * int(ns.astype(np.int64).sum())
+    out = {"workload": "uneven batch: %d transforms, N in 8..4096 with P ~ 1/log2(N), int64 offset table, "
+                       "uniform[-1,1) values, %.2f GiB in" % (count, total * 16 / GIB),
+           "count": count, "algorithmic_bytes": algo_bytes,
+           "per_size_counts": {str(n): int(np.sum(ns == n)) for n in inputs.SIZES}}
+    K = max(3, args.steps)
+    for mode, per_size in (("graph", False), ("per_size_launches", True)):
+        for _ in range(3):
+            plan(x, d_off, d_ns, out=y, stream=stream, per_size=per_size)
+        torch.cuda.synchronize()
+        barrier(world)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(K):
+            plan(x, d_off, d_ns, out=y, stream=stream, per_size=per_size)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = allreduce_max(a.elapsed_time(b), world) / K
+        hbm, _ = peaks()
+        out[mode] = {"ms": round(ms, 4), "fft_per_s": world * count / (ms * 1e-3),
+                     "hbm_gbs": round(algo_bytes / (ms * 1e-3) / 1e9, 1),
+                     "frac_hbm": round(algo_bytes / (ms * 1e-3) / 1e9 / hbm, 4)}
+    out["graph_speedup_vs_per_size"] = round(out["per_size_launches"]["ms"] / out["graph"]["ms"], 3)
+    out["gpu_launches_per_step"] = {"graph": 1 + 3 + len(inputs.SIZES),
+                                    "per_size_launches": 1 + 3 + int(sum(1 for n in inputs.SIZES if np.any(ns == n)))}
+    plan.close()
+    del x, y
+    return out
 
 
 def main():

@@ -16,7 +16,7 @@ from ._lib import (ENGINE_AUTO, ENGINE_DMMA, ENGINE_F64, ENGINE_FX, ENGINES, EXP
                    check, load, plan_query, plan_select)
 
 __all__ = ["fft", "fft_ptr", "fft_host", "fft_host_ptr", "plan_query", "plan_select", "autotune", "FftocError", "SIZES",
-           "ENGINES", "load", "auto_engine"]
+           "ENGINES", "load", "auto_engine", "UnevenPlan", "fft_uneven"]
 
 
 def _engine_id(engine):
@@ -92,6 +92,84 @@ def fft_host(x_host, out=None, engine="auto", device=0):
         fft_host_ptr(src.shape[-1], src.data_ptr(), out.data_ptr(), src.shape[0], stream.cuda_stream, engine)
         stream.synchronize()
     return out.numpy() if not isinstance(x_host, torch.Tensor) else out
+
+
+def _uneven_check(x, offsets, ns, out):
+    import torch
+
+    if not isinstance(x, torch.Tensor) or x.dtype != torch.complex128 or not x.is_cuda or not x.is_contiguous():
+        raise TypeError("x must be a contiguous complex128 CUDA tensor")
+    if offsets.dtype != torch.int64 or ns.dtype != torch.int32 or offsets.device != x.device or ns.device != x.device:
+        raise TypeError("offsets must be int64 and ns int32 tensors on x's device")
+    if offsets.numel() != ns.numel() or not offsets.is_contiguous() or not ns.is_contiguous():
+        raise ValueError("offsets and ns must be contiguous and of equal length")
+    if out is None:
+        out = torch.empty_like(x)
+    elif out.dtype != x.dtype or out.numel() != x.numel() or not out.is_contiguous() or out.device != x.device:
+        raise ValueError("out must match x")
+    return out
+
+
+class UnevenPlan:
+    """Mixed-size batches in one CUDA graph (fftoc_uneven_plan_*).
+
+    ``plan(x, offsets, ns)`` transforms, for every i, the ns[i] points of the
+    packed complex128 CUDA tensor ``x`` starting at element offsets[i] (int64
+    and int32 CUDA tensors).  ``per_size=True`` runs the comparison path (one
+    launch per size after a synchronous read of the per-size counts).
+    """
+
+    def __init__(self, max_count, engine="auto"):
+        import ctypes
+
+        self._L = load()
+        self._p = ctypes.c_void_p()
+        check(self._L.fftoc_uneven_plan_create(ctypes.byref(self._p), int(max_count), _engine_id(engine)))
+        self.max_count = int(max_count)
+
+    def __call__(self, x, offsets, ns, out=None, stream=None, per_size=False):
+        import torch
+
+        out = _uneven_check(x, offsets, ns, out)
+        if stream is None:
+            stream = torch.cuda.current_stream(x.device)
+        fn = self._L.fftoc_uneven_execute_per_size if per_size else self._L.fftoc_uneven_execute
+        with torch.cuda.device(x.device):
+            check(fn(self._p, x.data_ptr(), out.data_ptr(), offsets.data_ptr(), ns.data_ptr(), ns.numel(),
+                     stream.cuda_stream))
+        return out
+
+    def counts(self):
+        """Per-size transform counts of the last bucketing {n: count}."""
+        import ctypes
+
+        c = (ctypes.c_int64 * len(SIZES))()
+        check(self._L.fftoc_uneven_counts(self._p, c))
+        return {n: int(c[i]) for i, n in enumerate(SIZES)}
+
+    def close(self):
+        if self._p:
+            check(self._L.fftoc_uneven_plan_destroy(self._p))
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def fft_uneven(x, offsets, ns, out=None, stream=None):
+    """One-shot uneven batch (fftoc_c2c_fwd_uneven, plan cached per device)."""
+    import torch
+
+    out = _uneven_check(x, offsets, ns, out)
+    if stream is None:
+        stream = torch.cuda.current_stream(x.device)
+    with torch.cuda.device(x.device):
+        check(load().fftoc_c2c_fwd_uneven(x.data_ptr(), out.data_ptr(), offsets.data_ptr(), ns.data_ptr(), ns.numel(),
+                                          stream.cuda_stream))
+    return out
 
 
 def _make_size_entry(n):

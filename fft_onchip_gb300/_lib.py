@@ -41,6 +41,12 @@ EXPORTS = tuple(["fftoc_c2c_fwd_n%d" % n for n in SIZES]) + (
     "fftoc_status_string",
     "fftoc_last_error_string",
     "fftoc_version",
+    "fftoc_uneven_plan_create",
+    "fftoc_uneven_execute",
+    "fftoc_uneven_execute_per_size",
+    "fftoc_uneven_counts",
+    "fftoc_uneven_plan_destroy",
+    "fftoc_c2c_fwd_uneven",
 )
 
 
@@ -112,6 +118,17 @@ def load(path=None):
     L.fftoc_last_error_string.restype = ctypes.c_char_p
     L.fftoc_version.argtypes = []
     L.fftoc_version.restype = c_int
+    L.fftoc_uneven_plan_create.argtypes = [ctypes.POINTER(vp), i64, c_int]
+    L.fftoc_uneven_plan_create.restype = c_int
+    for f in (L.fftoc_uneven_execute, L.fftoc_uneven_execute_per_size):
+        f.argtypes = [vp, vp, vp, vp, vp, i64, vp]
+        f.restype = c_int
+    L.fftoc_uneven_counts.argtypes = [vp, ctypes.POINTER(i64)]
+    L.fftoc_uneven_counts.restype = c_int
+    L.fftoc_uneven_plan_destroy.argtypes = [vp]
+    L.fftoc_uneven_plan_destroy.restype = c_int
+    L.fftoc_c2c_fwd_uneven.argtypes = [vp, vp, vp, vp, i64, vp]
+    L.fftoc_c2c_fwd_uneven.restype = c_int
     _lib = L
     return L
 

@@ -233,6 +233,16 @@ void twiddle_tables(const KernelDesc& d, std::vector<double>& f64, std::vector<i
 int chosen_variant(int eng_slot, int idx) { return g_choice[eng_slot][idx].load(std::memory_order_relaxed); }
 int resolved_engine(int n, int engine) { return resolve_engine(n, engine); }
 fftoc_status set_error(fftoc_status st, const std::string& msg) { return fail(st, msg); }
+fftoc_status device_plan_resources(int slot, int idx, int var, const void** tw, int** err, int* sms) {
+  DeviceState* ds = nullptr;
+  fftoc_status st = device_state(&ds);
+  if (st != FFTOC_OK) return st;
+  if (var < 0 || var >= ds->var[slot][idx].count) return fail(FFTOC_ERR_INVALID_VALUE, "no such plan variant");
+  *tw = ds->tw[slot][idx][var];
+  *err = ds->err;
+  *sms = ds->sms;
+  return FFTOC_OK;
+}
 
 fftoc_status launch_fwd(int n, const double* in, double* out, int64_t batch, int engine, cudaStream_t stream,
                         int variant = -1) {
@@ -360,7 +370,8 @@ fftoc_status device_error_check() {
   if (h != 0) {
     e = cudaMemset(ds->err, 0, sizeof(int));
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(error flag)");
-    return fail(FFTOC_ERR_TIMEOUT, "a kernel's bounded wait for its prefetched tile gave up");
+    if (h & kErrTimeout) return fail(FFTOC_ERR_TIMEOUT, "a kernel's bounded wait for its prefetched tile gave up");
+    return fail(FFTOC_ERR_INVALID_VALUE, "an uneven batch skipped entries with an unsupported size or a negative offset");
   }
   return FFTOC_OK;
 }

@@ -240,35 +240,57 @@ struct Fft {
   }
 };
 
-// Engine-specific entry/exit: load raw points (binary64), convert, run the
-// passes, convert back and store.
-template <class E, class PL>
-__global__ void __launch_bounds__(Fft<E, PL>::THREADS, PL::MINB)
-fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long long batch,
-               const typename E::TW* __restrict__ tw, int* __restrict__ err) {
-  (void)err;  // no waits in this kernel; the argument keeps one launch signature
+// Where the transforms of one CTA tile live.  ContigTile: the batched entry
+// points, transform tile0 + j at element (tile0 + j) * N.  IndexedTile (the
+// uneven-batch kernel): transform j of the tile at element base[j], with the
+// bases staged in shared memory by the caller.
+template <int N>
+struct ContigTile {
+  const double2* __restrict__ in;
+  double2* __restrict__ out;
+  long long tile0, count;
+  __device__ __forceinline__ const double2* in_of(int j) const { return in + (tile0 + j) * N; }
+  __device__ __forceinline__ double2* out_of(int j) const { return out + (tile0 + j) * N; }
+  // element e of transform jj, idx = jj * N + e
+  __device__ __forceinline__ const double2* in_elem(int idx, int, int) const { return in + tile0 * N + idx; }
+  __device__ __forceinline__ double2* out_elem(int idx, int, int) const { return out + tile0 * N + idx; }
+};
+
+struct IndexedTile {
+  const double2* __restrict__ in;
+  double2* __restrict__ out;
+  const long long* base;  // shared memory, one entry per transform of the tile
+  long long tile0, count;
+  __device__ __forceinline__ const double2* in_of(int j) const { return in + base[j]; }
+  __device__ __forceinline__ double2* out_of(int j) const { return out + base[j]; }
+  __device__ __forceinline__ const double2* in_elem(int, int jj, int e) const { return in + base[jj] + e; }
+  __device__ __forceinline__ double2* out_elem(int, int jj, int e) const { return out + base[jj] + e; }
+};
+
+// One CTA tile: load raw points (binary64), convert, run the passes, convert
+// back and store.  Engine-specific entry/exit.
+template <class E, class PL, class Tile>
+__device__ __forceinline__ void fft_tile(const Tile& tl, const typename E::TW* __restrict__ tw,
+                                         unsigned char* smem_raw) {
   using F = Fft<E, PL>;
   using S = typename E::S;
   constexpr int N = PL::N, TPB = PL::TPB;
   constexpr int P = F::P, T = F::T, NS = F::NS;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   longlong2* sm = reinterpret_cast<longlong2*>(smem_raw);
 
   const int tid = threadIdx.x;
   const int j = tid / T;
   const int t = tid - j * T;
-  const long long tile0 = (long long)blockIdx.x * TPB;
-  const long long tr = tile0 + j;
-  const bool active = tr < batch;
-  const long long tile_elems = (min((long long)TPB, batch - tile0)) * N;
+  const long long tile0 = tl.tile0;
+  const bool active = tile0 + j < tl.count;
+  const long long tile_elems = (min((long long)TPB, tl.count - tile0)) * N;
 
   // ---- load raw binary64 points: point i of this thread is element t + T*i
   double2 raw[P];
   if constexpr (F::STAGED) {
-    const double2* src = in + tile0 * N;
     for (int idx = tid; idx < tile_elems; idx += F::THREADS) {
       const int jj = idx / N, e = idx - jj * N;
-      const double2 v = __ldg(src + idx);
+      const double2 v = __ldg(tl.in_elem(idx, jj, e));
       sm[F::slot(jj, e)] = make_longlong2(__double_as_longlong(v.x), __double_as_longlong(v.y));
     }
     __syncthreads();
@@ -278,7 +300,7 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
       raw[i] = make_double2(__longlong_as_double(v.x), __longlong_as_double(v.y));
     }
   } else {
-    const double2* src = in + tr * N + t;
+    const double2* src = tl.in_of(j) + t;  // in range or unused: loads are guarded
 #pragma unroll
     for (int i = 0; i < P; ++i) raw[i] = active ? __ldg(src + T * i) : make_double2(0.0, 0.0);
   }
@@ -358,21 +380,32 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
             make_longlong2(__double_as_longlong(v.x), __double_as_longlong(v.y));
       }
     __syncthreads();
-    double2* dst = out + tile0 * N;
     for (int idx = tid; idx < tile_elems; idx += F::THREADS) {
       const int jj = idx / N, e = idx - jj * N;
       const longlong2 v = sm[F::slot(jj, e)];
-      dst[idx] = make_double2(__longlong_as_double(v.x), __longlong_as_double(v.y));
+      *tl.out_elem(idx, jj, e) = make_double2(__longlong_as_double(v.x), __longlong_as_double(v.y));
     }
   } else {
     if (active) {
-      double2* dst = out + tr * N;
+      double2* dst = tl.out_of(j);
 #pragma unroll
       for (int b = 0; b < BL; ++b)
 #pragma unroll
         for (int m = 0; m < RL; ++m) dst[F::template dest<NS - 1>(t, b, m)] = result(b + BL * m);
     }
   }
+}
+
+
+// The batched kernel: CTA b transforms transforms [b*TPB, b*TPB + TPB).
+template <class E, class PL>
+__global__ void __launch_bounds__(Fft<E, PL>::THREADS, PL::MINB)
+fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long long batch,
+               const typename E::TW* __restrict__ tw, int* __restrict__ err) {
+  (void)err;  // no waits in this kernel; the argument keeps one launch signature
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const ContigTile<PL::N> tl{in, out, (long long)blockIdx.x * PL::TPB, batch};
+  fft_tile<E, PL>(tl, tw, smem_raw);
 }
 
 }  // namespace fftoc

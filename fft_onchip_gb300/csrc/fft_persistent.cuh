@@ -11,6 +11,7 @@
 // copies in flight and returns.
 #pragma once
 #include "fft_kernel.cuh"
+#include "internal.h"
 
 namespace fftoc {
 
@@ -56,7 +57,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
 }
 
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s
-constexpr int kErrTimeout = 1;
 
 template <class E, class PL, int NSTAGE>
 struct Persist {
@@ -125,7 +125,7 @@ fft_fwd_persistent(const double2* __restrict__ in, double2* __restrict__ out, lo
     const bool got = mbar_wait_bounded(&bars[s], phase, kWaitLimitNs);
     if (!__syncthreads_and(got)) {
       if (tid == 0) {
-        atomicExch(err, kErrTimeout);
+        atomicOr(err, kErrTimeout);
         // bounded drain of this CTA's copies still in flight
         for (int k = 0; k < NSTAGE; ++k) {
           const long long pend = tile + (long long)k * gridDim.x;

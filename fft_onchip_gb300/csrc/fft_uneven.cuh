@@ -1,0 +1,166 @@
+// fftoc — uneven batches: transforms of mixed sizes packed in one buffer and
+// described by an int64 offset table, run as one CUDA graph.
+//
+// The reference runs one size per launch (its harness stages UPB*FPU
+// transforms of a single executor per block, includes/testing.cuh:16-57, and
+// its benchmark driver loops over sizes, scripts/generate_bench.py:93-113).
+// Here one graph takes the whole mixed batch:
+//   1. uneven_hist     per 1024-entry chunk of the table, a histogram by size;
+//   2. uneven_scan     bucket starts and per-chunk bases (one CTA);
+//   3. uneven_scatter  stable bucketing: transform indices grouped by size, in
+//                      table order within a size;
+//   4. fft_uneven_kernel<E, PL>, one per size on parallel graph branches:
+//      persistent CTAs walk their size's bucket tile by tile, loading each
+//      transform from its own offset.
+// Steps 1-3 read the transform count from device memory, so the graph's
+// launch geometry depends only on the plan's maximum count.
+#pragma once
+#include "fft_kernel.cuh"
+#include "internal.h"
+
+namespace fftoc {
+
+constexpr int kUnevenChunk = 1024;              // table entries per bucketing CTA
+constexpr int kUnevenBins = 16;                 // 10 sizes + 1 "invalid" bin, padded
+constexpr int kUnevenInvalid = 10;
+
+// Argument block of one uneven execution (device memory; written by
+// uneven_set_args before each graph launch).
+struct UnevenArgs {
+  const double2* in;
+  double2* out;
+  const long long* offsets;   // complex-element offset of each transform (in and out)
+  const int* ns;              // size of each transform
+  long long count;            // transforms in the table
+  int* list;                  // bucketed transform indices [max_count]
+  int* chunk_base;            // [chunks][kUnevenBins]
+  int bucket_count[kUnevenBins];
+  int bucket_start[kUnevenBins];
+};
+
+static __global__ void uneven_set_args(UnevenArgs* a, const double2* in, double2* out, const long long* offsets,
+                                const int* ns, long long count) {
+  a->in = in;
+  a->out = out;
+  a->offsets = offsets;
+  a->ns = ns;
+  a->count = count;
+}
+
+__device__ __forceinline__ int uneven_bin(int n) {
+  // 8..4096 powers of two -> 0..9; anything else -> kUnevenInvalid
+  if (n < 8 || n > 4096 || (n & (n - 1))) return kUnevenInvalid;
+  return __ffs(n) - 4;
+}
+
+// bin of table entry i (valid size and non-negative offset), or -1 past the end
+__device__ __forceinline__ int uneven_entry_bin(const UnevenArgs& a, long long i) {
+  if (i >= a.count) return -1;
+  const int b = uneven_bin(__ldg(a.ns + i));
+  if (b == kUnevenInvalid) return b;
+  return __ldg(a.offsets + i) < 0 ? kUnevenInvalid : b;
+}
+
+static __global__ void __launch_bounds__(kUnevenChunk) uneven_hist(UnevenArgs* __restrict__ a, int* __restrict__ err) {
+  __shared__ int h[kUnevenBins];
+  if (threadIdx.x < kUnevenBins) h[threadIdx.x] = 0;
+  __syncthreads();
+  const long long chunk0 = (long long)blockIdx.x * kUnevenChunk;
+  if (chunk0 >= a->count) return;  // uniform per CTA
+  const int b = uneven_entry_bin(*a, chunk0 + threadIdx.x);
+  const unsigned peers = __match_any_sync(0xffffffffu, b);
+  if (b >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&h[b], __popc(peers));
+  __syncthreads();
+  if (threadIdx.x < kUnevenBins) a->chunk_base[blockIdx.x * kUnevenBins + threadIdx.x] = h[threadIdx.x];
+  if (threadIdx.x == kUnevenInvalid && h[kUnevenInvalid] > 0) atomicOr(err, kErrUnevenSkipped);
+}
+
+// One CTA of 32 x kUnevenBins threads: warp b scans bin b over the chunks.
+static __global__ void __launch_bounds__(32 * kUnevenBins) uneven_scan(UnevenArgs* __restrict__ a) {
+  __shared__ int total[kUnevenBins];
+  const int bin = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long count = a->count;
+  const int chunks = (int)((count + kUnevenChunk - 1) / kUnevenChunk);
+  int run = 0;
+  for (int c0 = 0; c0 < chunks; c0 += 32) {
+    const int c = c0 + lane;
+    const int v = c < chunks ? a->chunk_base[c * kUnevenBins + bin] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (c < chunks) a->chunk_base[c * kUnevenBins + bin] = run + x - v;  // exclusive, within the bin
+    run += __shfl_sync(0xffffffffu, x, 31);
+  }
+  if (lane == 0) total[bin] = run;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int b = 0; b < kUnevenBins; ++b) {
+      a->bucket_start[b] = s;
+      a->bucket_count[b] = b < kUnevenInvalid ? total[b] : 0;
+      s += total[b];
+    }
+  }
+}
+
+// Stable scatter: entry i goes to list[start(bin) + chunk base + rank of i
+// among the entries of its bin earlier in the chunk].
+static __global__ void __launch_bounds__(kUnevenChunk) uneven_scatter(UnevenArgs* __restrict__ a) {
+  __shared__ int wc[kUnevenChunk / 32][kUnevenBins];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long chunk0 = (long long)blockIdx.x * kUnevenChunk;
+  if (chunk0 >= a->count) return;
+  if (lane < kUnevenBins) wc[warp][lane] = 0;
+  __syncwarp();
+  const long long i = chunk0 + threadIdx.x;
+  const int b = uneven_entry_bin(*a, i);
+  const unsigned peers = __match_any_sync(0xffffffffu, b);
+  const int rank = __popc(peers & ((1u << lane) - 1u));
+  if (b >= 0 && rank == 0) wc[warp][b] = __popc(peers);
+  __syncthreads();
+  // exclusive scan over the 32 warps, one warp per bin
+  if (warp < kUnevenBins) {
+    const int v = wc[lane][warp];
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    __syncwarp();
+    wc[lane][warp] = x - v;
+  }
+  __syncthreads();
+  if (b >= 0 && b != kUnevenInvalid)
+    a->list[a->bucket_start[b] + a->chunk_base[blockIdx.x * kUnevenBins + b] + wc[warp][b] + rank] = (int)i;
+}
+
+// Persistent per-size kernel: CTAs stride over the tiles of bucket `bin`.
+template <class E, class PL>
+__global__ void __launch_bounds__(Fft<E, PL>::THREADS, PL::MINB)
+fft_uneven_kernel(const UnevenArgs* __restrict__ a, int bin, const typename E::TW* __restrict__ tw) {
+  using F = Fft<E, PL>;
+  constexpr int TPB = PL::TPB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  long long* base = reinterpret_cast<long long*>(smem_raw + F::SMEM);
+  const long long count = a->bucket_count[bin];
+  const int* list = a->list + a->bucket_start[bin];
+  const long long* offsets = a->offsets;
+  const IndexedTile proto{a->in, a->out, base, 0, count};
+  for (long long tile0 = (long long)blockIdx.x * TPB; tile0 < count; tile0 += (long long)gridDim.x * TPB) {
+    __syncthreads();  // the previous tile's readers of `base` and the staging buffer are done
+    if (threadIdx.x < TPB) {
+      const long long k = tile0 + threadIdx.x;
+      base[threadIdx.x] = k < count ? __ldg(offsets + __ldg(list + k)) : 0;
+    }
+    __syncthreads();
+    IndexedTile tl = proto;
+    tl.tile0 = tile0;
+    fft_tile<E, PL>(tl, tw, smem_raw);
+  }
+}
+
+}  // namespace fftoc

@@ -5,6 +5,8 @@
 #include <string>
 #include <vector>
 
+#include "../../include/fftoc.h"
+
 namespace fftoc {
 
 constexpr int kNumSizes = 10;
@@ -30,6 +32,10 @@ struct KernelDesc {
   int persistent = 0;        // 1: grid-stride persistent CTAs with TMA prefetch (extra error-flag argument)
   int stages = 0;            // shared-memory stages of the persistent kernel
   int blocks_per_sm = 0;     // resident CTAs per SM (filled at device set-up)
+  // uneven-batch kernel of the same plan (nullptr for TMA-prefetching plans)
+  const void* fn_uneven = nullptr;
+  int smem_uneven = 0;
+  int blocks_per_sm_uneven = 0;
 };
 
 constexpr int kMaxVariants = 8;
@@ -42,6 +48,14 @@ struct SizeVariants {
 // (kernels_<engine>.cu); variant 0 is the default choice.
 void describe_f64(SizeVariants* per_size);
 void describe_fx(SizeVariants* per_size);
+// Same walk over the plan list, filling only fn_uneven / smem_uneven
+// (kernels_uneven_<engine>.cu).
+void describe_uneven_f64(SizeVariants* per_size);
+void describe_uneven_fx(SizeVariants* per_size);
+
+// Device error-flag bits (the flag is returned by fftoc_device_error_check).
+constexpr int kErrTimeout = 1;        // a bounded wait for a prefetched tile gave up
+constexpr int kErrUnevenSkipped = 2;  // uneven-batch entries with a bad size or offset were skipped
 
 // api.cu accessors: compiled plans per engine slot (0 F64, 1 FX), twiddle
 // tables of a plan (16 bytes per entry: double2 / 4 x int32 limbs), the plan
@@ -51,5 +65,9 @@ const SizeVariants* compiled_variants(int eng_slot);
 void twiddle_tables(const KernelDesc& d, std::vector<double>& f64, std::vector<int>& fx);
 int chosen_variant(int eng_slot, int idx);
 int resolved_engine(int n, int engine);
+// The current device's twiddle table of plan (slot, size index, variant), its
+// error flag and SM count (device set-up on first use).
+fftoc_status device_plan_resources(int slot, int idx, int var, const void** tw, int** err, int* sms);
+fftoc_status set_error(fftoc_status st, const std::string& msg);
 
 }  // namespace fftoc

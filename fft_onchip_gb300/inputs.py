@@ -59,4 +59,35 @@ def loguniform(n, batch, seed=0, lo=1e-6, hi=1e6):
     return z.astype(np.complex128).reshape(batch, n)
 
 
+SIZES = (8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096)
+
+
+def uneven_sizes(count, seed=0):
+    """Transform sizes for an uneven batch: N from {8, ..., 4096} with
+    probability proportional to 1/log2(N) (inverse-CDF on a SplitMix64
+    uniform stream).  int32 array of length `count`."""
+    w = np.array([1.0 / np.log2(n) for n in SIZES])
+    cdf = np.cumsum(w / w.sum())
+    cdf[-1] = 1.0
+    u = _u01(seed ^ 0x1F83D9ABFB41BD6B, 0, count)
+    return np.asarray(SIZES, dtype=np.int32)[np.searchsorted(cdf, u, side="right")]
+
+
+def uneven_layout(ns):
+    """Back-to-back packing of transforms of sizes ns: (int64 offsets in
+    complex elements, total elements)."""
+    ns = np.asarray(ns, dtype=np.int64)
+    off = np.zeros(len(ns), dtype=np.int64)
+    if len(ns) > 1:
+        np.cumsum(ns[:-1], out=off[1:])
+    return off, int(ns.sum())
+
+
+def uniform_flat(total, seed=0):
+    """`total` complex values, re and im i.i.d. uniform [-1, 1) (the stream of
+    `uniform`)."""
+    v = (splitmix64(seed, 0, 2 * total) >> np.uint64(11)).astype(np.float64) * (2.0 ** -52) - 1.0
+    return v.view(np.complex128)
+
+
 FAMILIES = {"uniform": uniform, "normal": normal, "loguniform": loguniform}

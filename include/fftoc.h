@@ -161,10 +161,57 @@ fftoc_status fftoc_plan_select(int n, int engine, int variant);
 fftoc_status fftoc_autotune(int n, int engine, int64_t batch, fftoc_stream stream, int *best_variant,
                             float *best_ms);
 
+/* Uneven batches: `count` transforms of mixed sizes in one buffer (no
+ * counterpart in the reference, whose harness runs one size per launch,
+ * includes/testing.cuh:59-92, and whose benchmark loops over sizes,
+ * scripts/generate_bench.py:93-113).  Transform i has ns[i] points (8..4096,
+ * a power of two) starting at complex element offsets[i] of `in` and of
+ * `out`; in/out/offsets/ns are DEVICE pointers, in/out 16-byte aligned,
+ * offsets int64 (complex elements), ns int32.  Transforms must not overlap
+ * one another in `out` (in == out, in place, is allowed).  Entries with an
+ * unsupported size or a negative offset are skipped and raise the device
+ * error flag (fftoc_device_error_check -> FFTOC_ERR_INVALID_VALUE); offsets
+ * beyond the buffers are the caller's responsibility, as for `batch` in the
+ * per-size entry points.
+ *
+ * A plan owns the bucketing scratch (4 bytes per transform plus 64 bytes per
+ * 1024) and one CUDA graph: three bucketing kernels that group the transform
+ * indices by size (stable), then one persistent kernel per size on parallel
+ * graph branches, each using the plan currently chosen for its size
+ * (fftoc_plan_select / fftoc_autotune; TMA-prefetching plans fall back to
+ * the size's first plan without prefetch).  fftoc_uneven_execute enqueues a
+ * 1-thread argument kernel and the graph on `stream` and is asynchronous; it
+ * re-captures the graph when a size's plan choice changed.  One plan runs one
+ * batch at a time: executions of one plan must be ordered (same stream, or
+ * synchronised); use one plan per concurrent stream.  Create plans before
+ * any stream capture (creation allocates and captures). */
+typedef struct fftoc_uneven_plan_s *fftoc_uneven_plan;
+
+fftoc_status fftoc_uneven_plan_create(fftoc_uneven_plan *plan, int64_t max_count, int engine);
+fftoc_status fftoc_uneven_execute(fftoc_uneven_plan plan, const double *in, double *out, const int64_t *offsets,
+                                  const int32_t *ns, int64_t count, fftoc_stream stream);
+/* Same transforms without the graph: bucketing kernels, a synchronous read of
+ * the per-size counts, then one launch per non-empty size with one CTA per
+ * tile, all on `stream` (the comparison path; returns after enqueueing the
+ * last launch). */
+fftoc_status fftoc_uneven_execute_per_size(fftoc_uneven_plan plan, const double *in, double *out,
+                                           const int64_t *offsets, const int32_t *ns, int64_t count,
+                                           fftoc_stream stream);
+/* Per-size transform counts of the last bucketing (counts[10], sizes 8..4096);
+ * synchronous. */
+fftoc_status fftoc_uneven_counts(fftoc_uneven_plan plan, int64_t *counts);
+fftoc_status fftoc_uneven_plan_destroy(fftoc_uneven_plan plan);
+
+/* One-shot form: a plan cached per device, grown (re-created) when `count`
+ * exceeds its capacity; calls on one device must be ordered. */
+fftoc_status fftoc_c2c_fwd_uneven(const double *in, double *out, const int64_t *offsets, const int32_t *ns,
+                                  int64_t count, fftoc_stream stream);
+
 /* Device-side error flag of the current device: FFTOC_ERR_TIMEOUT if a
  * persistent kernel's bounded wait for a prefetched tile gave up since the
- * last check (its outputs are then incomplete), FFTOC_OK otherwise.  Clears
- * the flag.  Synchronous. */
+ * last check (its outputs are then incomplete), FFTOC_ERR_INVALID_VALUE if an
+ * uneven batch skipped entries (bad size or negative offset), FFTOC_OK
+ * otherwise.  Clears the flag.  Synchronous. */
 fftoc_status fftoc_device_error_check(void);
 
 /* Engine that FFTOC_ENGINE_AUTO resolves to for size n. */
