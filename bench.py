@@ -56,8 +56,9 @@ def parse():
     ap.add_argument("--gib", type=float, default=1.0, help="input GiB per size (1.0 = the sweep configuration)")
     ap.add_argument("--plan", default="", help="N:variant,... plan overrides (default: the library's choice)")
     ap.add_argument("--tuning", default="", help="tuning JSON written by fft_onchip_gb300.tune to apply")
-    ap.add_argument("--forms", default="uneven",
-                    help="extra workloads measured after the sweep (comma list of: uneven; empty for none)")
+    ap.add_argument("--forms", default="uneven,serve",
+                    help="extra workloads measured after the sweep (comma list of: uneven, serve; empty for none)")
+    ap.add_argument("--serve-rates", default="1e3,1e4,1e5,1e6", help="offered request rates (req/s) of the serving loop")
     ap.add_argument("--uneven-count", type=int, default=200000)
     return ap.parse_args()
 
@@ -355,6 +356,8 @@ def run_ours(args, world, rank, local):
     forms = {}
     if "uneven" in args.forms.split(","):
         forms["uneven"] = bench_uneven(args, torch, F, dev, stream, world)
+    if "serve" in args.forms.split(",") and rank == 0:
+        forms["serve"] = bench_serve(args, torch, F)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -425,6 +428,39 @@ def bench_uneven(args, torch, F, dev, stream, world):
                                     "per_size_launches": 1 + 3 + int(sum(1 for n in inputs.SIZES if np.any(ns == n)))}
     plan.close()
     del x, y
+    return out
+
+
+def bench_serve(args, torch, F):
+    """Serving loop: Poisson arrivals at each offered rate, each request 1..4096
+    transforms (log-uniform) of one N (uniform over 8..4096), N(0,1)-sized
+    values from pinned host memory; 8 GiB device pool with admission by
+    bytes; latency = completion - scheduled arrival."""
+    from fft_onchip_gb300 import inputs
+    from fft_onchip_gb300.serve import Server, latency_summary, make_trace
+    arena = 1 << 25  # complex values (512 MiB) per arena; the largest request is 2^24
+    h_in = torch.empty(arena, dtype=torch.complex128, pin_memory=True)
+    h_in.copy_(torch.randn(arena, dtype=torch.complex128, generator=torch.Generator().manual_seed(5)))
+    h_out = torch.empty(arena, dtype=torch.complex128, pin_memory=True)
+    srv = Server(pool_bytes=8 << 30, slots=4, max_batch_bytes=256 << 20, max_wait_us=50.0)
+    warm, _, _ = make_trace(1e4, 64, arena, seed=99)
+    srv.replay(warm, h_in, h_out)
+    out = {"workload": "Poisson arrivals; request = 1..4096 transforms (log-uniform) of one N uniform over "
+                       "8..4096; N(0,1) values in pinned host memory; 8 GiB device pool, admission by bytes; "
+                       "4 batches in flight, 256 MiB per batch, 50 us batching window",
+           "tag": "every request on the FP64 form (engine auto)", "rates": []}
+    for rate in [float(r) for r in args.serve_rates.split(",") if r]:
+        m = int(min(2000, max(200, rate * 0.4)))
+        items, transforms, nbytes = make_trace(rate, m, arena, seed=int(rate) % 1000003)
+        before = srv.stats()
+        lat, wall = srv.replay(items, h_in, h_out)
+        after = srv.stats()
+        row = {"offered_req_per_s": rate, "requests": m, "achieved_req_per_s": m / wall,
+               "fft_per_s": transforms / wall, "host_link_gbs_each_way": nbytes / wall / 1e9,
+               "batches": after["batches"] - before["batches"], "max_inflight_batches": after["max_inflight_batches"]}
+        row.update(latency_summary(lat))
+        out["rates"].append(row)
+    srv.close()
     return out
 
 

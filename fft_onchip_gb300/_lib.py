@@ -47,7 +47,36 @@ EXPORTS = tuple(["fftoc_c2c_fwd_n%d" % n for n in SIZES]) + (
     "fftoc_uneven_counts",
     "fftoc_uneven_plan_destroy",
     "fftoc_c2c_fwd_uneven",
+    "fftoc_server_config_default",
+    "fftoc_server_create",
+    "fftoc_server_submit",
+    "fftoc_server_poll",
+    "fftoc_server_wait",
+    "fftoc_server_stats",
+    "fftoc_server_replay",
+    "fftoc_server_destroy",
 )
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("pool_bytes", ctypes.c_int64), ("slots", ctypes.c_int), ("max_batch_bytes", ctypes.c_int64),
+                ("max_wait_us", ctypes.c_double)]
+
+
+class RequestTiming(ctypes.Structure):
+    _fields_ = [("submit_us", ctypes.c_double), ("launch_us", ctypes.c_double), ("done_us", ctypes.c_double),
+                ("status", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("batches", ctypes.c_int64), ("requests_done", ctypes.c_int64), ("transforms_done", ctypes.c_int64),
+                ("bytes_done", ctypes.c_int64), ("pool_bytes_in_use", ctypes.c_int64), ("pending", ctypes.c_int64),
+                ("max_inflight_batches", ctypes.c_int)]
+
+
+class ReplayItem(ctypes.Structure):
+    _fields_ = [("arrival_us", ctypes.c_double), ("n", ctypes.c_int), ("engine", ctypes.c_int),
+                ("count", ctypes.c_int64), ("in_offset", ctypes.c_int64), ("out_offset", ctypes.c_int64)]
 
 
 class PlanInfo(ctypes.Structure):
@@ -129,6 +158,23 @@ def load(path=None):
     L.fftoc_uneven_plan_destroy.restype = c_int
     L.fftoc_c2c_fwd_uneven.argtypes = [vp, vp, vp, vp, i64, vp]
     L.fftoc_c2c_fwd_uneven.restype = c_int
+    L.fftoc_server_config_default.argtypes = [ctypes.POINTER(ServerConfig)]
+    L.fftoc_server_config_default.restype = None
+    L.fftoc_server_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(ServerConfig)]
+    L.fftoc_server_create.restype = c_int
+    L.fftoc_server_submit.argtypes = [vp, c_int, i64, c_int, vp, vp, ctypes.POINTER(i64)]
+    L.fftoc_server_submit.restype = c_int
+    L.fftoc_server_poll.argtypes = [vp, i64, ctypes.POINTER(c_int), ctypes.POINTER(RequestTiming)]
+    L.fftoc_server_poll.restype = c_int
+    L.fftoc_server_wait.argtypes = [vp, i64, ctypes.c_double, ctypes.POINTER(RequestTiming)]
+    L.fftoc_server_wait.restype = c_int
+    L.fftoc_server_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
+    L.fftoc_server_stats.restype = c_int
+    L.fftoc_server_replay.argtypes = [vp, ctypes.POINTER(ReplayItem), i64, vp, vp, ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_double)]
+    L.fftoc_server_replay.restype = c_int
+    L.fftoc_server_destroy.argtypes = [vp]
+    L.fftoc_server_destroy.restype = c_int
     _lib = L
     return L
 

@@ -207,6 +207,73 @@ fftoc_status fftoc_uneven_plan_destroy(fftoc_uneven_plan plan);
 fftoc_status fftoc_c2c_fwd_uneven(const double *in, double *out, const int64_t *offsets, const int32_t *ns,
                                   int64_t count, fftoc_stream stream);
 
+/* Serving loop (no counterpart in the reference): continuous batching of FFT
+ * requests of mixed sizes from host memory.  A request is `count` transforms
+ * of one size n (interleaved complex doubles, 16-byte aligned host buffers,
+ * pinned memory for full-speed copies) and an engine.  A scheduler thread
+ * admits requests in arrival order into a device pool allocated once at
+ * creation (admission by bytes: a request waits until one free range of the
+ * pool holds it), packs requests of one engine into batches of up to
+ * max_batch_bytes, and runs each batch on one of `slots` streams: H2D copies
+ * into the pool, one uneven-batch graph over all its transforms, D2H copies.
+ * New batches are formed and launched while others run, as slots and pool
+ * memory free up.  A batch launches when it is full, when its oldest request
+ * has waited max_wait_us, or when nothing else is in flight.  A request's
+ * result is bit-identical whatever it was batched with.  The caller keeps
+ * h_in/h_out valid and h_out untouched until the request is done. */
+typedef struct {
+  int64_t pool_bytes;      /* device pool for request data (default 8 GiB)   */
+  int slots;               /* batches in flight, one stream each (default 4) */
+  int64_t max_batch_bytes; /* request bytes per batch (default 256 MiB)      */
+  double max_wait_us;      /* batching window (default 50 us)                */
+} fftoc_server_config;
+
+typedef struct {
+  double submit_us, launch_us, done_us; /* server clock (us since creation) */
+  fftoc_status status;
+} fftoc_request_timing;
+
+typedef struct {
+  int64_t batches, requests_done, transforms_done, bytes_done, pool_bytes_in_use, pending;
+  int max_inflight_batches;
+} fftoc_server_stats_t;
+
+typedef struct fftoc_server_s *fftoc_server;
+
+void fftoc_server_config_default(fftoc_server_config *cfg);
+/* Allocates the pool, per-slot streams, offset tables and uneven plans, and
+ * starts the scheduler thread (create before any stream capture). */
+fftoc_status fftoc_server_create(fftoc_server *server, const fftoc_server_config *cfg);
+/* Queue a request; returns at once with its id.  count*n*16 must fit in the
+ * pool and count <= max_batch_bytes/128. */
+fftoc_status fftoc_server_submit(fftoc_server server, int n, int64_t count, int engine, const double *h_in,
+                                 double *h_out, int64_t *request_id);
+/* done = 1 once h_out holds the result; the id is then released (poll or
+ * wait, once per id). */
+fftoc_status fftoc_server_poll(fftoc_server server, int64_t request_id, int *done, fftoc_request_timing *timing);
+/* Block until the request is done (FFTOC_ERR_TIMEOUT after timeout_s > 0). */
+fftoc_status fftoc_server_wait(fftoc_server server, int64_t request_id, double timeout_s,
+                               fftoc_request_timing *timing);
+fftoc_status fftoc_server_stats(fftoc_server server, fftoc_server_stats_t *stats);
+
+/* Load replay: submit items[i] at arrival_us after the call starts (a
+ * submitting loop on the calling thread), wait for all, and report each
+ * request's latency (completion minus scheduled arrival, us) and the wall
+ * time.  Requests read h_in_arena + in_offset and write h_out_arena +
+ * out_offset (complex elements); requests may share input ranges. */
+typedef struct {
+  double arrival_us;
+  int n;
+  int engine;
+  int64_t count;
+  int64_t in_offset;
+  int64_t out_offset;
+} fftoc_replay_item;
+fftoc_status fftoc_server_replay(fftoc_server server, const fftoc_replay_item *items, int64_t m,
+                                 const double *h_in_arena, double *h_out_arena, double *latency_us, double *wall_s);
+/* Finish the batches in flight, fail requests not yet started, free everything. */
+fftoc_status fftoc_server_destroy(fftoc_server server);
+
 /* Device-side error flag of the current device: FFTOC_ERR_TIMEOUT if a
  * persistent kernel's bounded wait for a prefetched tile gave up since the
  * last check (its outputs are then incomplete), FFTOC_ERR_INVALID_VALUE if an

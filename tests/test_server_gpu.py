@@ -1,0 +1,119 @@
+"""GPU tests of the serving loop (fftoc_server_*): every request's result
+matches the oracle, a request's result is bit-identical alone and inside a
+mix of concurrent requests (and equal to the per-size entry point), pool
+admission bounds the bytes on the device, and bad requests are refused."""
+import numpy as np
+import pytest
+
+from fft_onchip_gb300 import inputs
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-13
+
+
+def pinned(torch, a):
+    t = torch.empty(a.shape, dtype=torch.complex128, pin_memory=True)
+    t.copy_(torch.from_numpy(np.ascontiguousarray(a)))
+    return t
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint64)
+
+
+def test_alone_equals_in_mix_and_matches_oracle(cuda, fftoc_lib):
+    import fft_onchip_gb300 as F
+    from fft_onchip_gb300.serve import Server
+    srv = Server(pool_bytes=1 << 30, slots=3, max_batch_bytes=16 << 20, max_wait_us=200.0)
+    target = inputs.normal(256, 37, seed=77)
+    alone = srv.submit(pinned(cuda, target))
+    srv.wait(alone)
+    y_alone = alone.out.numpy().copy()
+    assert O.rel_l2(y_alone, O.fft_f64(target)) < TOL
+    # the same request inside a stream of mixed requests, submitted back to back
+    rng = np.random.default_rng(1)
+    reqs, xs = [], []
+    for i in range(60):
+        if i == 31:
+            x = target
+        else:
+            n = int(rng.choice(inputs.SIZES))
+            x = inputs.normal(n, int(rng.integers(1, 300)), seed=1000 + i)
+        xs.append(x)
+        reqs.append(srv.submit(pinned(cuda, x)))
+    for r in reqs:
+        srv.wait(r)
+    st = srv.stats()
+    assert st["requests_done"] == 61 and st["pool_bytes_in_use"] == 0 and st["pending"] == 0
+    assert st["batches"] < 61  # requests were batched together
+    y_mix = reqs[31].out.numpy()
+    assert np.array_equal(bits(y_mix), bits(y_alone))
+    ref = F.fft(cuda.from_numpy(target).cuda()).cpu().numpy()
+    assert np.array_equal(bits(y_mix), bits(ref))
+    for x, r in zip(xs, reqs):
+        assert O.rel_l2(r.out.numpy(), O.fft_f64(x)) < TOL
+    srv.close()
+
+
+def test_pool_admission_bounds_device_bytes(cuda, fftoc_lib):
+    from fft_onchip_gb300.serve import Server
+    # pool of 3 MiB: two 1.5 MiB requests fit, a third waits for memory
+    srv = Server(pool_bytes=3 << 20, slots=4, max_batch_bytes=1 << 20, max_wait_us=0.0)
+    xs = [inputs.uniform(512, 192, seed=s) for s in range(8)]  # 1.5 MiB each
+    reqs = [srv.submit(pinned(cuda, x)) for x in xs]
+    for x, r in zip(xs, reqs):
+        srv.wait(r)
+        assert O.rel_l2(r.out.numpy(), O.fft_f64(x)) < TOL
+    st = srv.stats()
+    assert st["requests_done"] == 8 and st["max_inflight_batches"] <= 2
+    srv.close()
+
+
+def test_refused_requests(cuda, fftoc_lib):
+    import fft_onchip_gb300 as F
+    from fft_onchip_gb300.serve import Server
+    srv = Server(pool_bytes=1 << 20, slots=1, max_batch_bytes=1 << 20)
+    with pytest.raises(F.FftocError) as e:
+        srv.submit(pinned(cuda, inputs.uniform(4096, 32, seed=1)))  # 2 MiB > pool
+    assert e.value.status_name == "FFTOC_ERR_INVALID_VALUE"
+    with pytest.raises(F.FftocError) as e:
+        srv.submit(pinned(cuda, inputs.uniform(100, 2, seed=1)))
+    assert e.value.status_name == "FFTOC_ERR_INVALID_SIZE"
+    with pytest.raises(F.FftocError):
+        Server(pool_bytes=1 << 20, slots=0)
+    srv.close()
+
+
+def test_poll_and_close_with_work_queued(cuda, fftoc_lib):
+    from fft_onchip_gb300.serve import Server
+    srv = Server(pool_bytes=64 << 20, slots=2, max_batch_bytes=8 << 20)
+    x = inputs.normal(1024, 100, seed=5)
+    r = srv.submit(pinned(cuda, x))
+    import time
+    t0 = time.time()
+    while not srv.poll(r):
+        assert time.time() - t0 < 60
+        time.sleep(0.001)
+    assert O.rel_l2(r.out.numpy(), O.fft_f64(x)) < TOL
+    for s in range(20):
+        srv.submit(pinned(cuda, inputs.normal(2048, 50, seed=s)))
+    srv.close()  # finishes batches in flight, fails the rest, returns
+
+
+def test_replay_reports_latencies(cuda, fftoc_lib):
+    from fft_onchip_gb300.serve import Server, latency_summary, make_trace
+    srv = Server(pool_bytes=1 << 30, slots=4)
+    arena = 1 << 24  # 256 MiB of complex values
+    h_in = cuda.empty(arena, dtype=cuda.complex128, pin_memory=True)
+    h_in.copy_(cuda.from_numpy(inputs.uniform_flat(arena, seed=2)))
+    h_out = cuda.empty(arena, dtype=cuda.complex128, pin_memory=True)
+    items, transforms, nbytes = make_trace(2e4, 200, arena, seed=3)
+    lat, wall = srv.replay(items, h_in, h_out)
+    assert len(lat) == 200 and np.all(lat > 0) and wall > 0
+    s = latency_summary(lat)
+    assert s["p99_ms"] >= s["p50_ms"] > 0
+    st = srv.stats()
+    assert st["requests_done"] == 200 and st["transforms_done"] == transforms
+    srv.close()
