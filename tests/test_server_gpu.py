@@ -26,29 +26,32 @@ def bits(a):
 def test_alone_equals_in_mix_and_matches_oracle(cuda, fftoc_lib):
     import fft_onchip_gb300 as F
     from fft_onchip_gb300.serve import Server
-    srv = Server(pool_bytes=1 << 30, slots=3, max_batch_bytes=16 << 20, max_wait_us=200.0)
+    # one stream slot: requests that arrive while a batch runs queue up and
+    # leave together in the next batch
+    srv = Server(pool_bytes=1 << 30, slots=1, max_batch_bytes=64 << 20, max_wait_us=200.0)
     target = inputs.normal(256, 37, seed=77)
     alone = srv.submit(pinned(cuda, target))
     srv.wait(alone)
     y_alone = alone.out.numpy().copy()
     assert O.rel_l2(y_alone, O.fft_f64(target)) < TOL
-    # the same request inside a stream of mixed requests, submitted back to back
+    # the same request inside a stream of mixed requests, submitted back to
+    # back behind a large one that keeps the slot busy
     rng = np.random.default_rng(1)
-    reqs, xs = [], []
+    xs = [inputs.normal(4096, 2048, seed=999)]
     for i in range(60):
         if i == 31:
-            x = target
+            xs.append(target)
         else:
             n = int(rng.choice(inputs.SIZES))
-            x = inputs.normal(n, int(rng.integers(1, 300)), seed=1000 + i)
-        xs.append(x)
-        reqs.append(srv.submit(pinned(cuda, x)))
+            xs.append(inputs.normal(n, int(rng.integers(1, 300)), seed=1000 + i))
+    hs = [pinned(cuda, x) for x in xs]
+    reqs = [srv.submit(h) for h in hs]
     for r in reqs:
         srv.wait(r)
     st = srv.stats()
-    assert st["requests_done"] == 61 and st["pool_bytes_in_use"] == 0 and st["pending"] == 0
-    assert st["batches"] < 61  # requests were batched together
-    y_mix = reqs[31].out.numpy()
+    assert st["requests_done"] == 62 and st["pool_bytes_in_use"] == 0 and st["pending"] == 0
+    assert st["batches"] < 40  # requests were batched together
+    y_mix = reqs[32].out.numpy()
     assert np.array_equal(bits(y_mix), bits(y_alone))
     ref = F.fft(cuda.from_numpy(target).cuda()).cpu().numpy()
     assert np.array_equal(bits(y_mix), bits(ref))
