@@ -22,7 +22,10 @@ STATUS_NAMES = {
 }
 
 ENGINE_AUTO, ENGINE_F64, ENGINE_FX, ENGINE_DMMA = 0, 1, 2, 3
-ENGINES = {"auto": ENGINE_AUTO, "f64": ENGINE_F64, "fx": ENGINE_FX, "dmma": ENGINE_DMMA}
+ENGINE_SPLIT_BF16X3, ENGINE_SPLIT_TF32X2 = 4, 5
+ENGINES = {"auto": ENGINE_AUTO, "f64": ENGINE_F64, "fx": ENGINE_FX, "dmma": ENGINE_DMMA,
+           "split_bf16x3": ENGINE_SPLIT_BF16X3, "split_tf32x2": ENGINE_SPLIT_TF32X2}
+SPLIT_BF16X3, SPLIT_TF32X2 = 1, 2
 
 SIZES = (8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096)
 
@@ -32,6 +35,7 @@ EXPORTS = tuple(["fftoc_c2c_fwd_n%d" % n for n in SIZES]) + (
     "fftoc_c2c_fwd_ex",
     "fftoc_c2c_fwd_host",
     "fftoc_c2c_fwd_host_noalloc",
+    "fftoc_c2c_fwd_split",
     "fftoc_plan_query",
     "fftoc_plan_query_variant",
     "fftoc_plan_select",
@@ -129,6 +133,8 @@ def load(path=None):
     L.fftoc_c2c_fwd_host.restype = c_int
     L.fftoc_c2c_fwd_host_noalloc.argtypes = [c_int, vp, vp, i64, c_int, vp]
     L.fftoc_c2c_fwd_host_noalloc.restype = c_int
+    L.fftoc_c2c_fwd_split.argtypes = [c_int, vp, vp, i64, c_int, vp]
+    L.fftoc_c2c_fwd_split.restype = c_int
     L.fftoc_plan_query.argtypes = [c_int, c_int, ctypes.POINTER(PlanInfo)]
     L.fftoc_plan_query.restype = c_int
     L.fftoc_plan_query_variant.argtypes = [c_int, c_int, c_int, ctypes.POINTER(PlanInfo)]

@@ -159,7 +159,10 @@ void init_device(DeviceState& ds) {
       for (int v = 0; v < ds.var[eng][i].count; ++v) {
         KernelDesc& d = ds.var[eng][i].v[v];
         cudaError_t e = cudaFuncSetAttribute(d.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, d.smem);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.blocks_per_sm, d.fn, d.threads, d.smem);
+        // persistent grids are sized from the resident CTAs per SM
+        if (e == cudaSuccess && d.persistent) e = fit_carveout(d.fn, d.threads, d.smem, &d.blocks_per_sm);
+        else if (e == cudaSuccess)
+          e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.blocks_per_sm, d.fn, d.threads, d.smem);
         if (e != cudaSuccess) {
           cudaGetLastError();
           ds.init_status = FFTOC_ERR_CUDA;
@@ -249,7 +252,7 @@ fftoc_status launch_fwd(int n, const double* in, double* out, int64_t batch, int
   const int idx = size_index(n);
   if (idx < 0) return fail(FFTOC_ERR_INVALID_SIZE, "n=" + std::to_string(n) + " is not one of 8,16,...,4096");
   if (batch < 0) return fail(FFTOC_ERR_INVALID_VALUE, "batch must be >= 0");
-  if (engine < FFTOC_ENGINE_AUTO || engine > FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_INVALID_VALUE, "unknown engine");
+  if (engine < FFTOC_ENGINE_AUTO || engine > kLastEngine) return fail(FFTOC_ERR_INVALID_VALUE, "unknown engine");
   if (batch == 0) return FFTOC_OK;
   if (!in || !out) return fail(FFTOC_ERR_INVALID_VALUE, "null buffer");
   if (((uintptr_t)in & 15) || ((uintptr_t)out & 15)) return fail(FFTOC_ERR_MISALIGNED, "buffers must be 16-byte aligned");
@@ -260,6 +263,7 @@ fftoc_status launch_fwd(int n, const double* in, double* out, int64_t batch, int
 
   const int eng = resolve_engine(n, engine);
   if (eng == FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_UNSUPPORTED, "DMMA engine not available for n=" + std::to_string(n));
+  if (is_split_engine(eng)) return launch_split(n, in, out, batch, split_kind_of(eng), stream);
   DeviceState* ds = nullptr;
   fftoc_status st = device_state(&ds);
   if (st != FFTOC_OK) return st;
@@ -287,7 +291,7 @@ fftoc_status launch_fwd_host(int n, const double* h_in, double* h_out, int64_t b
   const int idx = size_index(n);
   if (idx < 0) return fail(FFTOC_ERR_INVALID_SIZE, "n=" + std::to_string(n) + " is not one of 8,16,...,4096");
   if (batch < 0) return fail(FFTOC_ERR_INVALID_VALUE, "batch must be >= 0");
-  if (engine < FFTOC_ENGINE_AUTO || engine > FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_INVALID_VALUE, "unknown engine");
+  if (engine < FFTOC_ENGINE_AUTO || engine > kLastEngine) return fail(FFTOC_ERR_INVALID_VALUE, "unknown engine");
   if (batch == 0) return FFTOC_OK;
   if (!h_in || !h_out) return fail(FFTOC_ERR_INVALID_VALUE, "null buffer");
   if (((uintptr_t)h_in & 15) || ((uintptr_t)h_out & 15)) return fail(FFTOC_ERR_MISALIGNED, "buffers must be 16-byte aligned");
@@ -336,9 +340,13 @@ fftoc_status plan_query(int n, int engine, int variant, fftoc_plan_info* info) {
   const int idx = size_index(n);
   if (idx < 0) return fail(FFTOC_ERR_INVALID_SIZE, "n=" + std::to_string(n) + " is not one of 8,16,...,4096");
   if (!info) return fail(FFTOC_ERR_INVALID_VALUE, "null info");
-  if (engine < FFTOC_ENGINE_AUTO || engine > FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_INVALID_VALUE, "unknown engine");
+  if (engine < FFTOC_ENGINE_AUTO || engine > kLastEngine) return fail(FFTOC_ERR_INVALID_VALUE, "unknown engine");
   const int eng = resolve_engine(n, engine);
   if (eng == FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_UNSUPPORTED, "DMMA engine not available for n=" + std::to_string(n));
+  if (is_split_engine(eng)) {
+    if (variant > 0) return fail(FFTOC_ERR_INVALID_VALUE, "no such plan variant");
+    return split_plan_info(n, split_kind_of(eng), info);
+  }
   const int slot = eng == FFTOC_ENGINE_FX ? 1 : 0;
   const SizeVariants& sv = host_variants(slot)[idx];
   const int var = variant >= 0 ? variant : g_choice[slot][idx].load(std::memory_order_relaxed);

@@ -79,8 +79,9 @@ void setup(NoAllocDevice& nd, int dev) {
         KernelDesc& d = nd.var[slot][i].v[v];
         if ((e = cudaFuncSetAttribute(d.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, d.smem)) != cudaSuccess)
           return bad(e, "cudaFuncSetAttribute");
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.blocks_per_sm, d.fn, d.threads, d.smem)) !=
-            cudaSuccess)
+        if ((e = d.persistent ? fit_carveout(d.fn, d.threads, d.smem, &d.blocks_per_sm)
+                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.blocks_per_sm, d.fn, d.threads,
+                                                                              d.smem)) != cudaSuccess)
           return bad(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
         if (d.blocks_per_sm < 1) d.blocks_per_sm = 1;
         std::vector<double> f64;
@@ -117,7 +118,7 @@ fftoc_status launch_fwd_host_noalloc(int n, const double* h_in, double* h_out, i
   const int idx = size_index(n);
   if (idx < 0) return set_error(FFTOC_ERR_INVALID_SIZE, "n=" + std::to_string(n) + " is not one of 8,16,...,4096");
   if (batch < 0) return set_error(FFTOC_ERR_INVALID_VALUE, "batch must be >= 0");
-  if (engine < FFTOC_ENGINE_AUTO || engine > FFTOC_ENGINE_DMMA)
+  if (engine < FFTOC_ENGINE_AUTO || engine > kLastEngine)
     return set_error(FFTOC_ERR_INVALID_VALUE, "unknown engine");
   if (batch == 0) return FFTOC_OK;
   if (!h_in || !h_out) return set_error(FFTOC_ERR_INVALID_VALUE, "null buffer");

@@ -117,11 +117,33 @@ void CUDART_CB batch_done(void* p) {
   delete cd;
 }
 
-// Enqueue one batch on its slot (scheduler thread, lock NOT held).
-fftoc_status enqueue_batch(fftoc_server_s* s, int si, const std::vector<Request*>& rs, int engine_slot,
+// Enqueue one batch on its slot (scheduler thread, lock NOT held).  Plain
+// form: one uneven-batch graph over all the batch's transforms.  Split form:
+// each request is contiguous in the pool, one launch per request.
+fftoc_status enqueue_batch(fftoc_server_s* s, int si, const std::vector<Request*>& rs, int engine,
                            int64_t transforms) {
   Slot& sl = s->slots[si];
   cudaError_t e;
+  if (is_split_engine(engine)) {
+    for (const Request* r : rs) {
+      if ((e = cudaMemcpyAsync(s->pool_base + r->pool_off, r->h_in, (size_t)r->bytes, cudaMemcpyHostToDevice,
+                               sl.stream)) != cudaSuccess)
+        return cuda_fail(e, "cudaMemcpyAsync(request in)");
+      double* buf = reinterpret_cast<double*>(s->pool_base + r->pool_off);
+      const fftoc_status st = launch_split(r->n, buf, buf, r->count, split_kind_of(engine), sl.stream);
+      if (st != FFTOC_OK) return st;
+      if ((e = cudaMemcpyAsync(r->h_out, s->pool_base + r->pool_off, (size_t)r->bytes, cudaMemcpyDeviceToHost,
+                               sl.stream)) != cudaSuccess)
+        return cuda_fail(e, "cudaMemcpyAsync(request out)");
+    }
+    CallbackData* cd = new CallbackData{s, si};
+    if ((e = cudaLaunchHostFunc(sl.stream, batch_done, cd)) != cudaSuccess) {
+      delete cd;
+      return cuda_fail(e, "cudaLaunchHostFunc");
+    }
+    return FFTOC_OK;
+  }
+  const int engine_slot = engine == FFTOC_ENGINE_F64 ? 0 : 1;
   int64_t k = 0;
   for (const Request* r : rs) {
     const int64_t base = r->pool_off / 16;  // complex elements from the pool base
@@ -250,9 +272,8 @@ void scheduler(fftoc_server_s* s) {
       for (Request* r : batch) sl.reqs.push_back(r->id);
       s->batches += 1;
       if (inflight + 1 > s->max_inflight) s->max_inflight = inflight + 1;
-      const int eslot = resolved_engine(8, engine) == FFTOC_ENGINE_F64 ? 0 : 1;
       lk.unlock();
-      const fftoc_status st = enqueue_batch(s, si, batch, eslot, transforms);
+      const fftoc_status st = enqueue_batch(s, si, batch, engine, transforms);
       lk.lock();
       if (st != FFTOC_OK) {
         // the stream may hold part of the batch: drain it before reusing the ranges
@@ -354,10 +375,12 @@ fftoc_status submit(fftoc_server_s* s, int n, int64_t count, int engine, const d
   if (!s || !id) return set_error(FFTOC_ERR_INVALID_VALUE, "null pointer");
   if (size_index(n) < 0) return set_error(FFTOC_ERR_INVALID_SIZE, "n=" + std::to_string(n) + " is not one of 8,16,...,4096");
   if (count < 1) return set_error(FFTOC_ERR_INVALID_VALUE, "count must be >= 1");
-  if (engine < FFTOC_ENGINE_AUTO || engine > FFTOC_ENGINE_DMMA) return set_error(FFTOC_ERR_INVALID_VALUE, "unknown engine");
+  if (engine < FFTOC_ENGINE_AUTO || engine > kLastEngine) return set_error(FFTOC_ERR_INVALID_VALUE, "unknown engine");
   const int eng = resolved_engine(n, engine);
-  if (eng != FFTOC_ENGINE_F64 && eng != FFTOC_ENGINE_FX)
+  if (eng != FFTOC_ENGINE_F64 && eng != FFTOC_ENGINE_FX && !is_split_engine(eng))
     return set_error(FFTOC_ERR_UNSUPPORTED, "engine not available in the serving loop");
+  if (is_split_engine(eng) && !split_supported(n, split_kind_of(eng)))
+    return set_error(FFTOC_ERR_UNSUPPORTED, "no split-precision plan for n=" + std::to_string(n));
   if (!h_in || !h_out) return set_error(FFTOC_ERR_INVALID_VALUE, "null buffer");
   if (((uintptr_t)h_in & 15) || ((uintptr_t)h_out & 15)) return set_error(FFTOC_ERR_MISALIGNED, "buffers must be 16-byte aligned");
   const int64_t bytes = count * (int64_t)n * 16;

@@ -84,9 +84,7 @@ fftoc_status uneven_device(int dev, UnevenDevice** out) {
           KernelDesc& d = u.var[s][i].v[v];
           if (!d.fn_uneven) continue;
           cudaError_t e = cudaFuncSetAttribute(d.fn_uneven, cudaFuncAttributeMaxDynamicSharedMemorySize, d.smem_uneven);
-          if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.blocks_per_sm_uneven, d.fn_uneven, d.threads,
-                                                              d.smem_uneven);
+          if (e == cudaSuccess) e = fit_carveout(d.fn_uneven, d.threads, d.smem_uneven, &d.blocks_per_sm_uneven);
           if (e != cudaSuccess) {
             cudaGetLastError();
             u.status = FFTOC_ERR_CUDA;
@@ -221,7 +219,7 @@ fftoc_status plan_create(fftoc_uneven_plan* out, int64_t max_count, int engine) 
   *out = nullptr;
   if (max_count < 1 || max_count > 0x7FFFFFFFLL)
     return set_error(FFTOC_ERR_INVALID_VALUE, "max_count must be in [1, 2^31 - 1]");
-  if (engine < FFTOC_ENGINE_AUTO || engine > FFTOC_ENGINE_DMMA) return set_error(FFTOC_ERR_INVALID_VALUE, "unknown engine");
+  if (engine < FFTOC_ENGINE_AUTO || engine > kLastEngine) return set_error(FFTOC_ERR_INVALID_VALUE, "unknown engine");
   const int eng = resolved_engine(8, engine);
   if (eng != FFTOC_ENGINE_F64 && eng != FFTOC_ENGINE_FX)
     return set_error(FFTOC_ERR_UNSUPPORTED, "engine not available for uneven batches");

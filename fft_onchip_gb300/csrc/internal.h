@@ -53,6 +53,49 @@ void describe_fx(SizeVariants* per_size);
 void describe_uneven_f64(SizeVariants* per_size);
 void describe_uneven_fx(SizeVariants* per_size);
 
+// Split-precision form: one compiled plan per size (fn == nullptr: none).
+struct SplitDesc {
+  const void* fn = nullptr;
+  int threads = 0, tpb = 0, smem = 0, passes = 0;
+  int radix[4] = {1, 1, 1, 1};
+  int tw_entries = 0;  // FP32 twiddles (8 bytes each)
+  int b_bytes = 0;     // DFT-matrix operand slices
+  int esize = 0, slices = 0;
+  int blocks_per_sm = 0;
+};
+// kernels_split.cu; kind 1 = BF16x3, 2 = TF32x2
+void describe_split(int kind, SplitDesc* per_size);
+// api_split.cu; kind = fftoc_split_kind
+bool split_supported(int n, int kind);
+fftoc_status split_plan_info(int n, int kind, fftoc_plan_info* info);
+fftoc_status launch_split(int n, const double* in, double* out, int64_t batch, int kind, cudaStream_t stream);
+inline bool is_split_engine(int engine) {
+  return engine == FFTOC_ENGINE_SPLIT_BF16X3 || engine == FFTOC_ENGINE_SPLIT_TF32X2;
+}
+inline int split_kind_of(int engine) {
+  return engine == FFTOC_ENGINE_SPLIT_BF16X3 ? FFTOC_SPLIT_BF16X3 : FFTOC_SPLIT_TF32X2;
+}
+constexpr int kLastEngine = FFTOC_ENGINE_SPLIT_TF32X2;
+
+// Resident CTAs per SM of a persistent kernel, and the shared-memory carveout
+// that holds exactly that many (the rest of the SM's memory stays L1): the
+// occupancy is queried with the largest carveout, then the carveout is set
+// to the smallest percentage that still fits those CTAs.
+inline cudaError_t fit_carveout(const void* fn, int threads, int smem, int* blocks_per_sm) {
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       cudaSharedmemCarveoutMaxShared);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, threads, smem);
+  if (e != cudaSuccess) return e;
+  if (*blocks_per_sm < 1) *blocks_per_sm = 1;
+  int dev = 0, smem_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return e;
+  const long long need = (long long)*blocks_per_sm * (smem + 1024);  // + the per-CTA reserved kilobyte
+  int pct = (int)((100 * need + smem_sm - 1) / smem_sm);
+  if (pct > 100) pct = 100;
+  return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+}
+
 // Device error-flag bits (the flag is returned by fftoc_device_error_check).
 constexpr int kErrTimeout = 1;        // a bounded wait for a prefetched tile gave up
 constexpr int kErrUnevenSkipped = 2;  // uneven-batch entries with a bad size or offset were skipped

@@ -1,0 +1,47 @@
+// fftoc — split-precision form instantiations: one plan per size (radix-16
+// GEMM passes, a radix 2/4/8 last pass where N is not a power of 16), for
+// BF16x3 and TF32x2 operand splits.  256 threads = two groups of 128
+// butterfly rows per CTA, two CTAs per SM.
+#include "fft_split.cuh"
+#include "internal.h"
+
+namespace fftoc {
+namespace {
+
+template <int KIND, class PL>
+void add_split(SplitDesc& d) {
+  using SP = SplitPlan<KIND, PL, 2>;
+  d.fn = (const void*)&fft_split_kernel<KIND, PL, 2>;
+  d.threads = SP::THREADS;
+  d.tpb = PL::TPB;
+  d.smem = SP::SMEM;
+  d.passes = PL::S;
+  for (int i = 0; i < 4; ++i) d.radix[i] = PL::R[i];
+  d.tw_entries = PL::TW_COUNT;
+  d.b_bytes = SP::B_BYTES;
+  d.esize = SplitT<KIND>::ESIZE;
+  d.slices = SplitT<KIND>::SLICES;
+}
+
+template <int KIND>
+void describe(SplitDesc* d) {
+  // index = size index (8 has no radix-16 pass: left empty)
+  add_split<KIND, PlanT<16, 16, 256, 16, 1, 1, 1, 2>>(d[1]);
+  add_split<KIND, PlanT<32, 16, 128, 16, 2, 1, 1, 2>>(d[2]);
+  add_split<KIND, PlanT<64, 16, 64, 16, 4, 1, 1, 2>>(d[3]);
+  add_split<KIND, PlanT<128, 16, 32, 16, 8, 1, 1, 2>>(d[4]);
+  add_split<KIND, PlanT<256, 16, 16, 16, 16, 1, 1, 2>>(d[5]);
+  add_split<KIND, PlanT<512, 16, 8, 16, 16, 2, 1, 2>>(d[6]);
+  add_split<KIND, PlanT<1024, 16, 4, 16, 16, 4, 1, 2>>(d[7]);
+  add_split<KIND, PlanT<2048, 16, 2, 16, 16, 8, 1, 2>>(d[8]);
+  add_split<KIND, PlanT<4096, 16, 1, 16, 16, 16, 1, 2>>(d[9]);
+}
+
+}  // namespace
+
+void describe_split(int kind, SplitDesc* per_size) {
+  if (kind == kSplitBF16x3) describe<kSplitBF16x3>(per_size);
+  else describe<kSplitTF32x2>(per_size);
+}
+
+}  // namespace fftoc

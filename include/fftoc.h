@@ -65,9 +65,16 @@ typedef enum {
   FFTOC_ENGINE_FX = 2,   /* 64-bit block fixed point: per-transform power-of-two
                             scale, exact integer adds, 60-bit twiddles;
                             relative L2 error ~1e-15                             */
-  FFTOC_ENGINE_DMMA = 3  /* Karatsuba complex GEMM on FP64 mma.m8n8k4
+  FFTOC_ENGINE_DMMA = 3, /* Karatsuba complex GEMM on FP64 mma.m8n8k4
                             (the reference's tensor_utils.cuh:32-36 scheme)      */
+  FFTOC_ENGINE_SPLIT_BF16X3 = 4, /* split-precision form, 3 BF16 terms per
+                            operand on the tensor cores, FP32 accumulation and
+                            data (relative L2 error ~1e-7; n >= 16)              */
+  FFTOC_ENGINE_SPLIT_TF32X2 = 5  /* split-precision form, 2 TF32 terms     */
 } fftoc_engine;
+
+/* Operand splits of the split-precision form (fftoc_c2c_fwd_split). */
+typedef enum { FFTOC_SPLIT_BF16X3 = 1, FFTOC_SPLIT_TF32X2 = 2 } fftoc_split_kind;
 
 typedef struct CUstream_st *fftoc_stream; /* same type as cudaStream_t */
 
@@ -90,6 +97,20 @@ fftoc_status fftoc_c2c_fwd(int n, const double *in, double *out, int64_t batch, 
 /* Same, with an explicit engine. */
 fftoc_status fftoc_c2c_fwd_ex(int n, const double *in, double *out, int64_t batch, int engine,
                               fftoc_stream stream);
+
+/* Split-precision form (no binary64 counterpart in the reference, whose
+ * tensor path is FP64 DMMA with FP32 twiddles, tensor_fft_64.cuh:33-39).
+ * Every radix-16 pass of the plan is a GEMM on the tensor cores (tcgen05):
+ * butterfly inputs and the 16-point DFT matrix are split into 3 BF16 terms
+ * (FFTOC_SPLIT_BF16X3, the six term products with i + j <= 2) or 2 TF32
+ * terms (FFTOC_SPLIT_TF32X2, three products), accumulated in FP32; data
+ * between passes and the twiddle products are FP32; input and output are
+ * binary64, with an exact power-of-two scale per transform when its largest
+ * magnitude is outside [2^-60, 2^60].  Same arguments and conventions as
+ * fftoc_c2c_fwd; n = 16..4096 (FFTOC_ERR_UNSUPPORTED for n = 8).  Also
+ * reachable as engines FFTOC_ENGINE_SPLIT_* of fftoc_c2c_fwd_ex. */
+fftoc_status fftoc_c2c_fwd_split(int n, const double *in, double *out, int64_t batch, int kind,
+                                 fftoc_stream stream);
 
 /* Host buffers in and out (the reference harness's path: cudaMemcpy H2D,
  * launch, cudaMemcpy D2H — includes/testing.cuh:109-113,166-171).
