@@ -56,8 +56,8 @@ def parse():
     ap.add_argument("--gib", type=float, default=1.0, help="input GiB per size (1.0 = the sweep configuration)")
     ap.add_argument("--plan", default="", help="N:variant,... plan overrides (default: the library's choice)")
     ap.add_argument("--tuning", default="", help="tuning JSON written by fft_onchip_gb300.tune to apply")
-    ap.add_argument("--forms", default="uneven,serve",
-                    help="extra workloads measured after the sweep (comma list of: uneven, serve; empty for none)")
+    ap.add_argument("--forms", default="split,uneven,serve",
+                    help="extra workloads measured after the sweep (comma list of: split, uneven, serve; empty for none)")
     ap.add_argument("--serve-rates", default="1e3,1e4,1e5,1e6", help="offered request rates (req/s) of the serving loop")
     ap.add_argument("--uneven-count", type=int, default=200000)
     return ap.parse_args()
@@ -354,6 +354,8 @@ def run_ours(args, world, rank, local):
         del h_in, h_out
 
     forms = {}
+    if "split" in args.forms.split(","):
+        forms["split"] = bench_split(args, torch, F, dev, stream, world, per_n)
     if "uneven" in args.forms.split(","):
         forms["uneven"] = bench_uneven(args, torch, F, dev, stream, world)
     if "serve" in args.forms.split(",") and rank == 0:
@@ -384,6 +386,65 @@ def run_ours(args, world, rank, local):
             "forms": forms,
         }
         print(json.dumps(line), flush=True)
+
+
+def bench_split(args, torch, F, dev, stream, world, per_n):
+    """Split-precision form, N in {256, 512, 4096}, 1 GiB of complex128 per N:
+    throughput of BF16x3 and TF32x2 against the plain form (the sweep's
+    default engine) and the IEEE binary64 engine on the same buffers; error
+    against the binary64 oracle on 64-transform samples of two input
+    families, (a) re/im N(0,1) and (b) |z| log-uniform in [1e-6, 1e6] with
+    uniform phase."""
+    from fft_onchip_gb300 import inputs
+    from oracle import oracle as O
+    L = F.load()
+    hbm, _ = peaks()
+    K = max(3, args.steps)
+    out = {"workload": "split-precision form: N in {256,512,4096}, 1 GiB complex128 per N; errors on 64-transform "
+                       "samples of families (a) N(0,1) and (b) log-uniform magnitudes [1e-6,1e6], uniform phase",
+           "gate_rel_l2": 1e-11, "per_n": {}}
+    sptr = stream.cuda_stream
+
+    def timed(n, x, y, batch, eng):
+        for _ in range(3):
+            F.check(L.fftoc_c2c_fwd_ex(n, x.data_ptr(), y.data_ptr(), batch, eng, sptr))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(K):
+            F.check(L.fftoc_c2c_fwd_ex(n, x.data_ptr(), y.data_ptr(), batch, eng, sptr))
+        b.record(stream)
+        torch.cuda.synchronize()
+        return allreduce_max(a.elapsed_time(b), world) / K
+
+    for n in (256, 512, 4096):
+        batch = GIB // (16 * n)
+        g = torch.Generator(device=dev).manual_seed(77 + n)
+        x = torch.randn(batch, n, dtype=torch.complex128, device=dev, generator=g)
+        y = torch.empty_like(x)
+        row = {"batch": batch}
+        for name, eng in (("plain", F.ENGINE_AUTO), ("f64", F.ENGINE_F64), ("split_bf16x3", F.ENGINE_SPLIT_BF16X3),
+                          ("split_tf32x2", F.ENGINE_SPLIT_TF32X2)):
+            ms = timed(n, x, y, batch, eng)
+            gbs = 32.0 * n * batch / (ms * 1e-3) / 1e9
+            row[name] = {"ms": round(ms, 4), "fft_per_s": world * batch / (ms * 1e-3), "hbm_gbs": round(gbs, 1),
+                         "frac_hbm": round(gbs / hbm, 4)}
+        for name in ("split_bf16x3", "split_tf32x2"):
+            eng = F.ENGINES[name]
+            errs = {}
+            for fam, gen in (("a_normal", inputs.normal), ("b_loguniform", inputs.loguniform)):
+                xs = gen(n, 64, seed=n)
+                d = torch.from_numpy(xs).to(dev)
+                ys = F.fft(d, engine=eng).cpu().numpy()
+                ref = O.fft_f64(xs)
+                errs[fam] = {"rel_l2": O.rel_l2(ys, ref), "max_abs": float(np.max(np.abs(ys - ref))),
+                             "max_abs_ref": float(np.max(np.abs(ref)))}
+            row[name]["error"] = errs
+            row[name]["meets_gate"] = all(v["rel_l2"] <= 1e-11 for v in errs.values())
+            row[name]["speedup_vs_plain"] = round(row["plain"]["ms"] / row[name]["ms"], 3)
+            row[name]["speedup_vs_f64_engine"] = round(row["f64"]["ms"] / row[name]["ms"], 3)
+        out["per_n"][str(n)] = row
+        del x, y
+    return out
 
 
 def bench_uneven(args, torch, F, dev, stream, world):
@@ -443,15 +504,17 @@ def bench_serve(args, torch, F):
     h_in.copy_(torch.randn(arena, dtype=torch.complex128, generator=torch.Generator().manual_seed(5)))
     h_out = torch.empty(arena, dtype=torch.complex128, pin_memory=True)
     srv = Server(pool_bytes=8 << 30, slots=4, max_batch_bytes=256 << 20, max_wait_us=50.0)
-    warm, _, _ = make_trace(1e4, 64, arena, seed=99)
+    tags = (F.ENGINE_AUTO, F.ENGINE_SPLIT_BF16X3)
+    warm, _, _ = make_trace(1e4, 64, arena, seed=99, engines=tags)
     srv.replay(warm, h_in, h_out)
     out = {"workload": "Poisson arrivals; request = 1..4096 transforms (log-uniform) of one N uniform over "
                        "8..4096; N(0,1) values in pinned host memory; 8 GiB device pool, admission by bytes; "
                        "4 batches in flight, 256 MiB per batch, 50 us batching window",
-           "tag": "every request on the FP64 form (engine auto)", "rates": []}
+           "tag": "50/50 plain FP64 form (engine auto) / split form BF16x3 (8-point requests always plain)",
+           "rates": []}
     for rate in [float(r) for r in args.serve_rates.split(",") if r]:
         m = int(min(2000, max(200, rate * 0.4)))
-        items, transforms, nbytes = make_trace(rate, m, arena, seed=int(rate) % 1000003)
+        items, transforms, nbytes = make_trace(rate, m, arena, seed=int(rate) % 1000003, engines=tags)
         before = srv.stats()
         lat, wall = srv.replay(items, h_in, h_out)
         after = srv.stats()

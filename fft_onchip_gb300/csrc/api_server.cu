@@ -6,7 +6,8 @@
 //   - admits requests in arrival order into a fixed device pool (allocated
 //     once at creation) by bytes: a request enters a batch only when a free
 //     range of the pool holds it (pool.h);
-//   - packs admitted requests of one engine into a device batch (up to
+//   - packs admitted requests of one engine (the oldest pending request's;
+//     requests of other engines keep their place) into a device batch (up to
 //     max_batch_bytes) and runs it on one of `slots` streams: H2D copy of each
 //     request into its pool range, the batch's offset table, one uneven-batch
 //     graph (fftoc_uneven_execute) over all its transforms, D2H copy of each
@@ -246,14 +247,18 @@ void scheduler(fftoc_server_s* s) {
         waiting_window = true;
         break;
       }
-      // admit in arrival order: same engine, batch bytes and transforms
-      // within limits, each request into a free pool range
+      // admit in arrival order the requests of the oldest request's engine
+      // (others keep their place), batch bytes and transforms within limits,
+      // each into a free pool range; stop at the first that does not fit
       const int engine = head.engine;
       std::vector<Request*> batch;
       int64_t bytes = 0, transforms = 0;
-      while (!s->pending.empty()) {
-        Request& r = s->reqs[s->pending.front()];
-        if (r.engine != engine) break;
+      for (auto it = s->pending.begin(); it != s->pending.end();) {
+        Request& r = s->reqs[*it];
+        if (r.engine != engine) {
+          ++it;
+          continue;
+        }
         if (!batch.empty() && (bytes + r.bytes > s->cfg.max_batch_bytes || transforms + r.count > s->max_count)) break;
         const int64_t off = s->pool->alloc(r.bytes);
         if (off < 0) break;  // wait for memory to free up
@@ -263,7 +268,7 @@ void scheduler(fftoc_server_s* s) {
         bytes += r.bytes;
         transforms += r.count;
         batch.push_back(&r);
-        s->pending.pop_front();
+        it = s->pending.erase(it);
       }
       if (batch.empty()) break;
       Slot& sl = s->slots[si];

@@ -97,7 +97,8 @@ class Server:
 def make_trace(rate, m, arena_elems, seed=0, engines=(_lib.ENGINE_AUTO,)):
     """m requests with Poisson arrivals at `rate` per second: count log-uniform
     in 1..4096, N uniform over 8..4096, engine drawn uniformly from `engines`
-    (a 50/50 tag with two entries).  Inputs and outputs are ranges of arenas of
+    (a 50/50 tag with two entries; split-form tags on N = 8 run on the plain
+    form, which the split form does not cover).  Inputs and outputs are ranges of arenas of
     `arena_elems` complex values (requests may share them).  Returns
     (ReplayItem array, total transforms, total bytes one way)."""
     rng = np.random.default_rng(seed)
@@ -107,6 +108,9 @@ def make_trace(rate, m, arena_elems, seed=0, engines=(_lib.ENGINE_AUTO,)):
     count = np.clip(count, 1, 4096)
     n = np.asarray(SIZES)[rng.integers(0, len(SIZES), size=m)]
     eng = np.asarray(engines)[rng.integers(0, len(engines), size=m)]
+    # the split-precision form starts at N = 16: 8-point requests run on the plain form
+    split = np.isin(eng, (_lib.ENGINE_SPLIT_BF16X3, _lib.ENGINE_SPLIT_TF32X2))
+    eng = np.where(split & (n == 8), _lib.ENGINE_AUTO, eng)
     items = (_lib.ReplayItem * m)()
     transforms = 0
     nbytes = 0

@@ -234,8 +234,9 @@ fftoc_status fftoc_c2c_fwd_uneven(const double *in, double *out, const int64_t *
  * pinned memory for full-speed copies) and an engine.  A scheduler thread
  * admits requests in arrival order into a device pool allocated once at
  * creation (admission by bytes: a request waits until one free range of the
- * pool holds it), packs requests of one engine into batches of up to
- * max_batch_bytes, and runs each batch on one of `slots` streams: H2D copies
+ * pool holds it), packs requests of the oldest pending request's engine
+ * into batches of up to max_batch_bytes (requests of other engines keep
+ * their place), and runs each batch on one of `slots` streams: H2D copies
  * into the pool, one uneven-batch graph over all its transforms, D2H copies.
  * New batches are formed and launched while others run, as slots and pool
  * memory free up.  A batch launches when it is full, when its oldest request

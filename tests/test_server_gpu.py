@@ -120,3 +120,32 @@ def test_replay_reports_latencies(cuda, fftoc_lib):
     st = srv.stats()
     assert st["requests_done"] == 200 and st["transforms_done"] == transforms
     srv.close()
+
+
+def test_split_tagged_requests_in_the_mix(cuda, fftoc_lib):
+    """Requests tagged with the split-precision form run on it (error of the
+    form, not binary64), the others on the plain form, in one stream."""
+    import fft_onchip_gb300 as F
+    from fft_onchip_gb300.serve import Server
+    srv = Server(pool_bytes=256 << 20, slots=2, max_batch_bytes=8 << 20)
+    xs, reqs, engs = [], [], []
+    for i in range(24):
+        n = (16, 256, 4096)[i % 3]
+        eng = "split_bf16x3" if i % 2 else "auto"
+        x = inputs.normal(n, 7 + i, seed=300 + i)
+        xs.append(x)
+        engs.append(eng)
+        reqs.append(srv.submit(pinned(cuda, x), engine=eng))
+    for x, r, eng in zip(xs, reqs, engs):
+        srv.wait(r)
+        err = O.rel_l2(r.out.numpy(), O.fft_f64(x))
+        if eng == "auto":
+            assert err < TOL
+        else:
+            assert 1e-12 < err < 1e-6
+            ref = F.fft(cuda.from_numpy(x).cuda(), engine=eng).cpu().numpy()
+            assert np.array_equal(bits(r.out.numpy()), bits(ref))
+    with pytest.raises(F.FftocError) as e:
+        srv.submit(pinned(cuda, inputs.normal(8, 4, seed=1)), engine="split_bf16x3")
+    assert e.value.status_name == "FFTOC_ERR_UNSUPPORTED"
+    srv.close()
