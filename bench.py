@@ -56,8 +56,9 @@ def parse():
     ap.add_argument("--gib", type=float, default=1.0, help="input GiB per size (1.0 = the sweep configuration)")
     ap.add_argument("--plan", default="", help="N:variant,... plan overrides (default: the library's choice)")
     ap.add_argument("--tuning", default="", help="tuning JSON written by fft_onchip_gb300.tune to apply")
-    ap.add_argument("--forms", default="split,uneven,serve",
-                    help="extra workloads measured after the sweep (comma list of: split, uneven, serve; empty for none)")
+    ap.add_argument("--forms", default="split,uneven,serve,onchip",
+                    help="extra workloads measured after the sweep (comma list of: split, uneven, serve, onchip; "
+                         "empty for none)")
     ap.add_argument("--serve-rates", default="1e3,1e4,1e5,1e6", help="offered request rates (req/s) of the serving loop")
     ap.add_argument("--uneven-count", type=int, default=200000)
     return ap.parse_args()
@@ -360,6 +361,8 @@ def run_ours(args, world, rank, local):
         forms["uneven"] = bench_uneven(args, torch, F, dev, stream, world)
     if "serve" in args.forms.split(",") and rank == 0:
         forms["serve"] = bench_serve(args, torch, F)
+    if "onchip" in args.forms.split(",") and rank == 0:
+        forms["onchip"] = bench_onchip(args, torch, F)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -444,6 +447,19 @@ def bench_split(args, torch, F, dev, stream, world, per_n):
             row[name]["speedup_vs_f64_engine"] = round(row["f64"]["ms"] / row[name]["ms"], 3)
         out["per_n"][str(n)] = row
         del x, y
+    return out
+
+
+def bench_onchip(args, torch, F):
+    """On-chip repeat mode (the reference's own timing method,
+    includes/testing.cuh:94-127): microseconds per in-shared-memory pass over
+    32 x SMs transforms, t(1100 repeats) - t(100 repeats) over 1000."""
+    from fft_onchip_gb300 import onchip
+    out = {"workload": "on-chip repeat mode: (32 x SMs) transforms per pass resident in shared memory, "
+                       "(t(1100) - t(100)) / 1000 per pass, no HBM traffic in the difference", "per_n": {}}
+    for n in (8, 64, 128, 256, 512, 4096):
+        r = onchip.time_onchip(n, F.ENGINE_AUTO)
+        out["per_n"][str(n)] = {k: r[k] for k in ("us_per_pass", "ffts_per_s", "transforms_per_block", "blocks")}
     return out
 
 

@@ -59,6 +59,8 @@ EXPORTS = tuple(["fftoc_c2c_fwd_n%d" % n for n in SIZES]) + (
     "fftoc_server_stats",
     "fftoc_server_replay",
     "fftoc_server_destroy",
+    "fftoc_onchip_plan",
+    "fftoc_onchip_run",
 )
 
 
@@ -181,6 +183,10 @@ def load(path=None):
     L.fftoc_server_replay.restype = c_int
     L.fftoc_server_destroy.argtypes = [vp]
     L.fftoc_server_destroy.restype = c_int
+    L.fftoc_onchip_plan.argtypes = [c_int, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
+    L.fftoc_onchip_plan.restype = c_int
+    L.fftoc_onchip_run.argtypes = [c_int, c_int, vp, i64, c_int, vp]
+    L.fftoc_onchip_run.restype = c_int
     _lib = L
     return L
 

@@ -254,6 +254,7 @@ struct ContigTile {
   // element e of transform jj, idx = jj * N + e
   __device__ __forceinline__ const double2* in_elem(int idx, int, int) const { return in + tile0 * N + idx; }
   __device__ __forceinline__ double2* out_elem(int idx, int, int) const { return out + tile0 * N + idx; }
+  __device__ __forceinline__ static double2 load(const double2* p) { return __ldg(p); }
 };
 
 struct IndexedTile {
@@ -265,6 +266,21 @@ struct IndexedTile {
   __device__ __forceinline__ double2* out_of(int j) const { return out + base[j]; }
   __device__ __forceinline__ const double2* in_elem(int, int jj, int e) const { return in + base[jj] + e; }
   __device__ __forceinline__ double2* out_elem(int, int jj, int e) const { return out + base[jj] + e; }
+  __device__ __forceinline__ static double2 load(const double2* p) { return __ldg(p); }
+};
+
+// The on-chip repeat harness: the tile's transforms resident in shared
+// memory (`buf`, TPB * N points, transformed in place), loaded with plain
+// shared loads.
+template <int N>
+struct SmemTile {
+  double2* buf;
+  long long tile0, count;  // tile0 = 0, count = TPB
+  __device__ __forceinline__ const double2* in_of(int j) const { return buf + j * N; }
+  __device__ __forceinline__ double2* out_of(int j) const { return buf + j * N; }
+  __device__ __forceinline__ const double2* in_elem(int idx, int, int) const { return buf + idx; }
+  __device__ __forceinline__ double2* out_elem(int idx, int, int) const { return buf + idx; }
+  __device__ __forceinline__ static double2 load(const double2* p) { return *p; }
 };
 
 // One CTA tile: load raw points (binary64), convert, run the passes, convert
@@ -291,7 +307,7 @@ __device__ __forceinline__ void fft_tile(const Tile& tl, const typename E::TW* _
   if constexpr (F::STAGED) {
     for (int idx = tid; idx < tile_elems; idx += F::THREADS) {
       const int jj = idx / N, e = idx - jj * N;
-      const double2 v = __ldg(tl.in_elem(idx, jj, e));
+      const double2 v = Tile::load(tl.in_elem(idx, jj, e));
       sm[F::slot(jj, e)] = make_longlong2(__double_as_longlong(v.x), __double_as_longlong(v.y));
     }
     __syncthreads();
@@ -303,7 +319,7 @@ __device__ __forceinline__ void fft_tile(const Tile& tl, const typename E::TW* _
   } else {
     const double2* src = tl.in_of(j) + t;  // in range or unused: loads are guarded
 #pragma unroll
-    for (int i = 0; i < P; ++i) raw[i] = active ? __ldg(src + T * i) : make_double2(0.0, 0.0);
+    for (int i = 0; i < P; ++i) raw[i] = active ? Tile::load(src + T * i) : make_double2(0.0, 0.0);
   }
 
   S re[P], im[P];

@@ -36,6 +36,9 @@ struct KernelDesc {
   const void* fn_uneven = nullptr;
   int smem_uneven = 0;
   int blocks_per_sm_uneven = 0;
+  // on-chip repeat kernel of the same plan (nullptr for TMA-prefetching plans)
+  const void* fn_onchip = nullptr;
+  int smem_onchip = 0;
 };
 
 constexpr int kMaxVariants = 8;
@@ -52,6 +55,8 @@ void describe_fx(SizeVariants* per_size);
 // (kernels_uneven_<engine>.cu).
 void describe_uneven_f64(SizeVariants* per_size);
 void describe_uneven_fx(SizeVariants* per_size);
+void describe_onchip_f64(SizeVariants* per_size);
+void describe_onchip_fx(SizeVariants* per_size);
 
 // Split-precision form: one compiled plan per size (fn == nullptr: none).
 struct SplitDesc {

@@ -296,6 +296,19 @@ fftoc_status fftoc_server_replay(fftoc_server server, const fftoc_replay_item *i
 /* Finish the batches in flight, fail requests not yet started, free everything. */
 fftoc_status fftoc_server_destroy(fftoc_server server);
 
+/* On-chip repeat harness (the reference's timing mode: testing::fft_tester
+ * and run_perf_tests, includes/testing.cuh:16-127).  Each of `blocks` CTAs
+ * copies its transforms_per_block transforms (from data + block * tpb * n)
+ * into shared memory, transforms them in place `repeats` times with the plan
+ * the library uses for (n, engine) (the whole per-transform computation,
+ * binary64 conversion included; TMA-prefetching plans fall back to the
+ * size's first plan without prefetch), and copies them back.  Differencing
+ * the times of two repeat counts gives the on-chip cost of one pass, as the
+ * reference reports it.  `data` holds blocks * tpb * n complex values (device
+ * memory).  Binary64 and fixed-point engines. */
+fftoc_status fftoc_onchip_plan(int n, int engine, int *transforms_per_block, int *variant);
+fftoc_status fftoc_onchip_run(int n, int engine, double *data, int64_t blocks, int repeats, fftoc_stream stream);
+
 /* Device-side error flag of the current device: FFTOC_ERR_TIMEOUT if a
  * persistent kernel's bounded wait for a prefetched tile gave up since the
  * last check (its outputs are then incomplete), FFTOC_ERR_INVALID_VALUE if an
