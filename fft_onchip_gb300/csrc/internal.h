@@ -83,19 +83,24 @@ inline int split_kind_of(int engine) {
 constexpr int kLastEngine = FFTOC_ENGINE_SPLIT_TF32X2;
 
 // Resident CTAs per SM of a persistent kernel, and the shared-memory carveout
-// that holds exactly that many (the rest of the SM's memory stays L1): the
-// occupancy is queried with the largest carveout, then the carveout is set
-// to the smallest percentage that still fits those CTAs.
+// that holds exactly that many (the rest of the SM's memory stays L1).  The
+// occupancy query does not apply a function's carveout preference, so the
+// CTAs are the smaller of the register/thread/barrier limit (queried without
+// shared memory) and the shared-memory limit of the largest carveout; the
+// carveout is then set to the smallest percentage of the SM's shared memory
+// that holds them.
 inline cudaError_t fit_carveout(const void* fn, int threads, int smem, int* blocks_per_sm) {
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                       cudaSharedmemCarveoutMaxShared);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, threads, smem);
+  int dev = 0, smem_sm = 0, reserved = 0, by_regs = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&by_regs, fn, threads, 0);
   if (e != cudaSuccess) return e;
-  if (*blocks_per_sm < 1) *blocks_per_sm = 1;
-  int dev = 0, smem_sm = 0;
-  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-  if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return e;
-  const long long need = (long long)*blocks_per_sm * (smem + 1024);  // + the per-CTA reserved kilobyte
+  const int by_smem = smem_sm / (smem + reserved);
+  int b = by_regs < by_smem ? by_regs : by_smem;
+  if (b < 1) b = 1;
+  *blocks_per_sm = b;
+  const long long need = (long long)b * (smem + reserved);
   int pct = (int)((100 * need + smem_sm - 1) / smem_sm);
   if (pct > 100) pct = 100;
   return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct);

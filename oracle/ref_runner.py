@@ -8,6 +8,7 @@ shared memory = 16 bytes per staged point.
 
     python -m oracle.ref_runner fixtures   # writes tests/golden/ref_out_*.npz
     python -m oracle.ref_runner timing     # on-chip us/pass like testing.cuh:94-127
+    python -m oracle.ref_runner stream     # one pass over 1 GiB in HBM: GB/s
 
 Fixtures record the reference's ACTUAL outputs on seeded inputs; the CPU
 tests pin the oracle's restatements and conventions against them.
@@ -131,9 +132,40 @@ def timing(sm_multiplier=32):
     return out
 
 
+def stream(gib=1.0, reps=5):
+    """Each executor streamed over a 1 GiB batch once per launch (copy in,
+    one transform, copy out: the harness with inner_repeats = 1), timed with
+    CUDA events; GB/s counts one complex128 read and write per point."""
+    import torch
+    drv = Driver()
+    out = {}
+    for name, (n, threads, staged) in EXECUTORS.items():
+        per_block = staged // n
+        batch = int(gib * (1 << 30)) // (16 * n)
+        batch -= batch % per_block
+        blocks = batch // per_block
+        d = torch.randn(batch, n, dtype=torch.complex128, device="cuda")
+        drv.launch(name, d.data_ptr(), blocks, 1)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            drv.launch(name, d.data_ptr(), blocks, 1)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / reps
+        out[name] = {"n": n, "batch": batch, "ms": ms, "ffts_per_s": batch / (ms * 1e-3),
+                     "hbm_gbs": 32.0 * n * batch / (ms * 1e-3) / 1e9}
+        print(json.dumps({name: out[name]}), flush=True)
+        del d
+    return out
+
+
 if __name__ == "__main__":
     what = sys.argv[1] if len(sys.argv) > 1 else "fixtures"
     if what == "fixtures":
         fixtures()
+    elif what == "stream":
+        stream()
     else:
         timing()
