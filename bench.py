@@ -373,8 +373,10 @@ def run_ours(args, world, rank, local):
 
     if rank == 0:
         resolved = sorted({F.plan_query(n, eng)["engine"] for n in sizes})
-        dtype = "int64 block fixed point (complex128 in/out)" if resolved == [F.ENGINE_FX] else (
-            "f64" if resolved == [F.ENGINE_F64] else "mixed f64/int64")
+        names = {F.ENGINE_FX: "int64 block fixed point (complex128 in/out)", F.ENGINE_F64: "f64",
+                 F.ENGINE_SPLIT_BF16X3: "bf16x3 split on tensor cores, fp32 accumulation (complex128 in/out)",
+                 F.ENGINE_SPLIT_TF32X2: "tf32x2 split on tensor cores, fp32 accumulation (complex128 in/out)"}
+        dtype = names.get(resolved[0], "mixed") if len(resolved) == 1 else "mixed"
         line = {
             "metric": METRIC, "value": value, "unit": "FFT/s", "n_gpus": world, "steps": K,
             "warmup": max(3, args.warmup), "ms_per_step": t_ms / K, "higher_is_better": True, "scaling": "weak",

@@ -28,9 +28,13 @@
  *
  * Parity status: the reference ships no golden vectors, no fixtures and no
  * known-answer tests (its only check, src/gpu_fft.cu:41-66, prints an MSE
- * against cuFFTDx, which is absent here), so these restatements are checked
- * against the mathematics (naive DFT, analytic known answers) and against
- * numpy.fft; see oracle/README for what pins what.
+ * against cuFFTDx, which is absent here).  These restatements are checked
+ * against the mathematics (naive DFT, analytic known answers), against
+ * numpy.fft, and against the reference's own executors run on a GPU:
+ * oracle/ref_runner.py launches them (compiled unmodified from the
+ * reference's headers by oracle/build_ref.py) and recorded their outputs in
+ * tests/golden/ref_out_*.npz, which tests/test_reference_pinning.py compares
+ * with orc_ref_tensor / orc_ref_legacy8 / orc_ref_legacy16.
  */
 #define _GNU_SOURCE
 #include <math.h>
