@@ -84,18 +84,28 @@ constexpr int kLastEngine = FFTOC_ENGINE_SPLIT_TF32X2;
 
 // Resident CTAs per SM of a persistent kernel, and the shared-memory carveout
 // that holds exactly that many (the rest of the SM's memory stays L1).  The
-// occupancy query does not apply a function's carveout preference, so the
-// CTAs are the smaller of the register/thread/barrier limit (queried without
-// shared memory) and the shared-memory limit of the largest carveout; the
-// carveout is then set to the smallest percentage of the SM's shared memory
-// that holds them.
+// occupancy query applies neither a function's carveout preference nor, for
+// kernels that use tcgen05 (it returns 1 for them at any size), the actual
+// limits, so the CTAs are computed here: the smallest of the register-file
+// limit (registers per thread rounded to the 256-register warp allocation
+// unit, 64K registers per SM), the thread limit (2048 per SM) and the
+// shared-memory limit of the largest carveout.  The carveout is then set to
+// the smallest percentage of the SM's shared memory that holds them.
 inline cudaError_t fit_carveout(const void* fn, int threads, int smem, int* blocks_per_sm) {
-  int dev = 0, smem_sm = 0, reserved = 0, by_regs = 0;
+  int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0, threads_sm = 0;
+  cudaFuncAttributes fa;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&by_regs, fn, threads, 0);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, fn);
   if (e != cudaSuccess) return e;
+  const int warps = (threads + 31) / 32;
+  const int regs_warp = ((fa.numRegs * 32 + 255) / 256) * 256;
+  int by_regs = regs_warp > 0 ? regs_sm / (regs_warp * warps) : 32;
+  const int by_threads = threads_sm / (warps * 32);
+  if (by_threads < by_regs) by_regs = by_threads;
   const int by_smem = smem_sm / (smem + reserved);
   int b = by_regs < by_smem ? by_regs : by_smem;
   if (b < 1) b = 1;
