@@ -82,7 +82,11 @@ struct SplitPlan {
   static constexpr int DATA_BYTES = TPB * NP * 8;
   static constexpr int RED_OFF = DATA_OFF + DATA_BYTES;  // per-transform exponent scratch
   static constexpr int BAR_OFF = RED_OFF + ((TPB * 4 + 15) / 16) * 16;
-  static constexpr int SMEM = BAR_OFF + 16;  // mbarrier + TMEM address slot
+  static constexpr int SMEM = BAR_OFF + 8 * G + 8;  // one mbarrier per group + TMEM address slot
+  // a transform's threads lie inside one 128-row group: the groups need no
+  // CTA-wide barrier inside a tile
+  static constexpr bool GROUP_LOCAL = T <= 128;
+  static_assert(G <= 2, "named barriers 1 and 2 serve the two groups");
   static constexpr int TMEM_COLS = 32 * G < 32 ? 32 : 32 * G;
   static constexpr int MMAS = K::NPAIRS * (32 / K::KMMA);
   static_assert((TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM allocation is a power of two");
@@ -248,16 +252,32 @@ struct SplitCtx {
   unsigned char* sA;
   unsigned char* sB;
   float2* data;
-  unsigned long long* bar;
+  unsigned long long* bar;  // one per group
   const float2* tw;
   unsigned tmem, idesc, phase;
   int tid, g, row, lane_block, j, t;
+  bool failed;  // a bounded wait gave up (the tile loop ends after the tile)
 };
 
+// Barrier over the threads that share data inside a tile: the thread's
+// 128-row group when transforms do not span groups, else the CTA.
+template <bool GROUP_LOCAL>
+__device__ __forceinline__ void tile_sync(int g) {
+  if constexpr (GROUP_LOCAL) {
+    // immediate barrier ids (a register id would reserve all 16 named barriers)
+    if (g == 0) asm volatile("bar.sync 1, 128;" ::: "memory");
+    else asm volatile("bar.sync 2, 128;" ::: "memory");
+  } else {
+    __syncthreads();
+  }
+}
+
 // Pass s of the plan on the thread's 16 points; the last pass stores to
-// `dst` (transform base, binary64).  Returns false when a bounded wait gave up.
+// `dst` (transform base, binary64).  A bounded wait that gives up sets
+// c.failed; the passes still run their barriers so every thread reaches the
+// end of the tile.
 template <int KIND, class PL, int G, int s>
-__device__ __forceinline__ bool split_pass(SplitCtx& c, float (&re)[16], float (&im)[16], double2* dst, bool active,
+__device__ __forceinline__ void split_pass(SplitCtx& c, float (&re)[16], float (&im)[16], double2* dst, bool active,
                                            int unshift, bool scaled) {
   using SP = SplitPlan<KIND, PL, G>;
   using K = SplitT<KIND>;
@@ -290,30 +310,27 @@ __device__ __forceinline__ bool split_pass(SplitCtx& c, float (&re)[16], float (
     store_slices<KIND, SP::A_SLICE>(c.sA + c.g * K::SLICES * SP::A_SLICE, c.row, re, im);
     fence_proxy_async_smem();
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    if (c.tid == 0) {
+    tile_sync<SP::GROUP_LOCAL>(c.g);
+    if (c.row == 0) {
+      // row 0 of each group issues that group's MMAs and commits them to its mbarrier
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const unsigned a0 = smem_u32(c.sA), b0 = smem_u32(c.sB);
+      const unsigned a0 = smem_u32(c.sA + c.g * K::SLICES * SP::A_SLICE), b0 = smem_u32(c.sB);
 #pragma unroll
-      for (int gg = 0; gg < G; ++gg) {
+      for (int q = 0; q < K::NPAIRS; ++q)
 #pragma unroll
-        for (int q = 0; q < K::NPAIRS; ++q)
-#pragma unroll
-          for (int kk = 0; kk < 32 / K::KMMA; ++kk) {
-            // K elements [kk*KMMA, kk*KMMA + KMMA) = 16-byte chunks 2kk, 2kk+1
-            const unsigned aa = a0 + (gg * K::SLICES + K::pair_x(q)) * SP::A_SLICE + kk * 256;
-            const unsigned bb = b0 + K::pair_f(q) * SP::B_SLICE + kk * 256;
-            umma<KIND>(c.tmem + 32 * gg, umma_desc(aa, 128, L::KC * 128), umma_desc(bb, 128, L::KC * 128), c.idesc,
-                       (q | kk) != 0);
-          }
-      }
+        for (int kk = 0; kk < 32 / K::KMMA; ++kk) {
+          // K elements [kk*KMMA, kk*KMMA + KMMA) = 16-byte chunks 2kk, 2kk+1
+          const unsigned aa = a0 + K::pair_x(q) * SP::A_SLICE + kk * 256;
+          const unsigned bb = b0 + K::pair_f(q) * SP::B_SLICE + kk * 256;
+          umma<KIND>(c.tmem + 32 * c.g, umma_desc(aa, 128, L::KC * 128), umma_desc(bb, 128, L::KC * 128), c.idesc,
+                     (q | kk) != 0);
+        }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       smem_u32(c.bar))
+                       smem_u32(c.bar + c.g))
                    : "memory");
     }
-    const bool ok = mbar_wait_bounded(c.bar, c.phase, kWaitLimitNs);
+    if (!c.failed && !mbar_wait_bounded(c.bar + c.g, c.phase, kWaitLimitNs)) c.failed = true;
     c.phase ^= 1;
-    if (!__syncthreads_and(ok)) return false;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     float d[32];
     tmem_ld32(c.tmem + ((unsigned)(c.lane_block * 32) << 16) + 32 * c.g, d);
@@ -349,8 +366,9 @@ __device__ __forceinline__ bool split_pass(SplitCtx& c, float (&re)[16], float (
         const int k = tp & (p - 1);
         c.data[SP::slot(c.j, (tp - k) * R + k + m * p)] = make_float2(re[b + Bq * m], im[b + Bq * m]);
       }
-    __syncthreads();
-    return split_pass<KIND, PL, G, s + 1>(c, re, im, dst, active, unshift, scaled);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");  // this pass's TMEM reads precede the next MMAs
+    tile_sync<SP::GROUP_LOCAL>(c.g);
+    split_pass<KIND, PL, G, s + 1>(c, re, im, dst, active, unshift, scaled);
   } else {
     if (active) {
 #pragma unroll
@@ -363,7 +381,6 @@ __device__ __forceinline__ bool split_pass(SplitCtx& c, float (&re)[16], float (
           dst[(tp - k) * R + k + m * p] = scaled ? make_double2(ldexp(xr, unshift), ldexp(xi, unshift)) : make_double2(xr, xi);
         }
     }
-    return true;
   }
 }
 
@@ -376,7 +393,7 @@ fft_split_kernel(const double2* __restrict__ in, double2* __restrict__ out, long
   constexpr int N = PL::N, TPB = PL::TPB, T = PL::T;
   extern __shared__ __align__(1024) unsigned char smem_split[];
   int* red = reinterpret_cast<int*>(smem_split + SP::RED_OFF);
-  unsigned* tslot = reinterpret_cast<unsigned*>(smem_split + SP::BAR_OFF + 8);
+  unsigned* tslot = reinterpret_cast<unsigned*>(smem_split + SP::BAR_OFF + 8 * G);
 
   SplitCtx c;
   c.sA = smem_split;
@@ -395,7 +412,7 @@ fft_split_kernel(const double2* __restrict__ in, double2* __restrict__ out, long
   // constant DFT-matrix slices, TMEM, mbarrier
   for (int i = c.tid; i < SP::B_BYTES / 16; i += SP::THREADS) reinterpret_cast<uint4*>(c.sB)[i] = __ldg(bmat + i);
   if (c.tid == 0) {
-    mbar_init(c.bar, 1);
+    for (int gg = 0; gg < G; ++gg) mbar_init(c.bar + gg, 1);
     mbar_fence_init();
   }
   if (warp == 0) {
@@ -410,6 +427,7 @@ fft_split_kernel(const double2* __restrict__ in, double2* __restrict__ out, long
   c.tmem = *tslot;
   c.idesc = (1u << 4) | (K::FMT << 7) | (K::FMT << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
   c.phase = 0;
+  c.failed = false;
 
   const long long ntiles = (batch + TPB - 1) / TPB;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -450,12 +468,14 @@ fft_split_kernel(const double2* __restrict__ in, double2* __restrict__ out, long
       re[i] = f64_to_f32_int(raw[i].x);
       im[i] = f64_to_f32_int(raw[i].y);
     }
-    if (!split_pass<KIND, PL, G, 0>(c, re, im, out + tr * N, active, -shift, scaled)) {
+    split_pass<KIND, PL, G, 0>(c, re, im, out + tr * N, active, -shift, scaled);
+    // exchange buffer and exponent scratch free for the next tile; stop after
+    // a bounded wait gave up anywhere in the CTA
+    if (__syncthreads_or(c.failed)) {
       if (c.tid == 0) atomicOr(err, kErrTimeout);
-      mbar_wait_bounded(c.bar, c.phase ^ 1, kWaitLimitNs);  // bounded drain of the MMAs in flight
+      mbar_wait_bounded(c.bar + c.g, c.phase ^ 1, kWaitLimitNs);  // bounded drain of the MMAs in flight
       break;
     }
-    __syncthreads();  // exchange buffer and exponent scratch free for the next tile
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
