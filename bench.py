@@ -395,8 +395,9 @@ def run_ours(args, world, rank, local):
 
 def bench_split(args, torch, F, dev, stream, world, per_n):
     """Split-precision form, N in {256, 512, 4096}, 1 GiB of complex128 per N:
-    throughput of BF16x3 and TF32x2 against the plain form (the sweep's
-    default engine) and the IEEE binary64 engine on the same buffers; error
+    throughput of BF16x3, TF32x2 and the exact-slice form against the plain
+    form (the sweep's default engine) and the IEEE binary64 engine on the
+    same buffers; error
     against the binary64 oracle on 64-transform samples of two input
     families, (a) re/im N(0,1) and (b) |z| log-uniform in [1e-6, 1e6] with
     uniform phase."""
@@ -428,12 +429,12 @@ def bench_split(args, torch, F, dev, stream, world, per_n):
         y = torch.empty_like(x)
         row = {"batch": batch}
         for name, eng in (("plain", F.ENGINE_AUTO), ("f64", F.ENGINE_F64), ("split_bf16x3", F.ENGINE_SPLIT_BF16X3),
-                          ("split_tf32x2", F.ENGINE_SPLIT_TF32X2)):
+                          ("split_tf32x2", F.ENGINE_SPLIT_TF32X2), ("split_exact", F.ENGINE_SPLIT_EXACT)):
             ms = timed(n, x, y, batch, eng)
             gbs = 32.0 * n * batch / (ms * 1e-3) / 1e9
             row[name] = {"ms": round(ms, 4), "fft_per_s": world * batch / (ms * 1e-3), "hbm_gbs": round(gbs, 1),
                          "frac_hbm": round(gbs / hbm, 4)}
-        for name in ("split_bf16x3", "split_tf32x2"):
+        for name in ("split_bf16x3", "split_tf32x2", "split_exact"):
             eng = F.ENGINES[name]
             errs = {}
             for fam, gen in (("a_normal", inputs.normal), ("b_loguniform", inputs.loguniform)):

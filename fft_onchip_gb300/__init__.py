@@ -12,8 +12,9 @@ tensor, forward (exp(-2*pi*i*n*k/N)), unnormalised, natural order, like
 ``fft::tensor_fft_64<CT,64>`` run by the reference harness
 (includes/testing.cuh:16-57).
 """
-from ._lib import (ENGINE_AUTO, ENGINE_DMMA, ENGINE_F64, ENGINE_FX, ENGINE_SPLIT_BF16X3, ENGINE_SPLIT_TF32X2, ENGINES,
-                   EXPORTS, SIZES, FftocError, autotune, check, load, plan_query, plan_select)
+from ._lib import (ENGINE_AUTO, ENGINE_DMMA, ENGINE_F64, ENGINE_FX, ENGINE_SPLIT_BF16X3, ENGINE_SPLIT_EXACT,
+                   ENGINE_SPLIT_TF32X2, ENGINES, EXPORTS, SIZES, FftocError, autotune, check, load, plan_query,
+                   plan_select)
 
 __all__ = ["fft", "fft_ptr", "fft_host", "fft_host_ptr", "plan_query", "plan_select", "autotune", "FftocError", "SIZES",
            "ENGINES", "load", "auto_engine", "UnevenPlan", "fft_uneven"]

@@ -22,10 +22,11 @@ STATUS_NAMES = {
 }
 
 ENGINE_AUTO, ENGINE_F64, ENGINE_FX, ENGINE_DMMA = 0, 1, 2, 3
-ENGINE_SPLIT_BF16X3, ENGINE_SPLIT_TF32X2 = 4, 5
+ENGINE_SPLIT_BF16X3, ENGINE_SPLIT_TF32X2, ENGINE_SPLIT_EXACT = 4, 5, 6
 ENGINES = {"auto": ENGINE_AUTO, "f64": ENGINE_F64, "fx": ENGINE_FX, "dmma": ENGINE_DMMA,
-           "split_bf16x3": ENGINE_SPLIT_BF16X3, "split_tf32x2": ENGINE_SPLIT_TF32X2}
-SPLIT_BF16X3, SPLIT_TF32X2 = 1, 2
+           "split_bf16x3": ENGINE_SPLIT_BF16X3, "split_tf32x2": ENGINE_SPLIT_TF32X2,
+           "split_exact": ENGINE_SPLIT_EXACT}
+SPLIT_BF16X3, SPLIT_TF32X2, SPLIT_EXACT = 1, 2, 3
 
 SIZES = (8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096)
 

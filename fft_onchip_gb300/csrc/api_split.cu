@@ -12,7 +12,8 @@
 namespace fftoc {
 namespace {
 
-constexpr int kKinds = 2;  // [0] BF16x3, [1] TF32x2
+constexpr int kKinds = 3;  // [0] BF16x3, [1] TF32x2, [2] exact slices
+int kind_index(int kind) { return kind - 1; }
 
 struct SplitDevice {
   std::once_flag once;
@@ -33,6 +34,7 @@ const SplitDesc* host_split(int k) {
   std::call_once(once, [] {
     describe_split(1, table[0]);
     describe_split(2, table[1]);
+    describe_split(3, table[2]);
   });
   return table[k];
 }
@@ -92,6 +94,39 @@ std::vector<unsigned char> dft16_operand(int esize, int slices) {
   return out;
 }
 
+// The same matrix for the exact-slice form: entries scaled by 2^47 (rounded
+// from long double) and cut into six balanced 8-bit digits, most significant
+// first, as BF16.
+std::vector<unsigned char> dft16_exact_operand() {
+  const int row_bytes = 64, kc = 4, per_chunk = 8;
+  std::vector<unsigned char> out((size_t)6 * 32 * row_bytes, 0);
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (int c = 0; c < 32; ++c)
+    for (int k = 0; k < 32; ++k) {
+      const int cc = c & 15, kk = k & 15;
+      const long double ang = -2.0L * pi * (long double)((cc * kk) % 16) / 16.0L;
+      const long double fr = cosl(ang), fi = sinl(ang);
+      long double v;
+      if (c < 16) v = k < 16 ? fr : -fi;
+      else v = k < 16 ? fi : fr;
+      long long t = llroundl(v * 140737488355328.0L);  // 2^47
+      int dig[6];
+      for (int q = 5; q >= 1; --q) {
+        const int d = (int)(signed char)(t & 0xFF);
+        dig[q] = d;
+        t = (t - d) >> 8;
+      }
+      dig[0] = (int)t;  // |t| <= 128
+      for (int q = 0; q < 6; ++q) {
+        const size_t off = (size_t)q * 32 * row_bytes +
+                           (size_t)(((c >> 3) * kc + k / per_chunk) * 128 + (c & 7) * 16 + (k % per_chunk) * 2);
+        const uint16_t h = bf16_rn((float)dig[q]);  // exact: |digit| <= 128
+        memcpy(&out[off], &h, 2);
+      }
+    }
+  return out;
+}
+
 void setup(SplitDevice& sd, int dev) {
   auto bad = [&](cudaError_t e, const char* what) {
     cudaGetLastError();
@@ -114,7 +149,7 @@ void setup(SplitDevice& sd, int dev) {
   sd.err = err;
   for (int k = 0; k < kKinds; ++k) {
     const SplitDesc* h = host_split(k);
-    const std::vector<unsigned char> b = dft16_operand(k == 0 ? 2 : 4, k == 0 ? 3 : 2);
+    const std::vector<unsigned char> b = k == 2 ? dft16_exact_operand() : dft16_operand(k == 0 ? 2 : 4, k == 0 ? 3 : 2);
     if ((e = cudaMalloc(&sd.bmat[k], b.size())) != cudaSuccess) return bad(e, "cudaMalloc(split matrix)");
     if ((e = cudaMemcpy(sd.bmat[k], b.data(), b.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
       return bad(e, "cudaMemcpy(split matrix)");
@@ -138,10 +173,20 @@ void setup(SplitDevice& sd, int dev) {
       std::vector<double> f64;
       std::vector<int> fx;
       twiddle_tables(kd, f64, fx);
+      const void* src;
+      size_t bytes;
       std::vector<float> f32(f64.size() > 0 ? f64.size() : 2, 0.f);
-      for (size_t q = 0; q < f64.size(); ++q) f32[q] = (float)f64[q];
-      if ((e = cudaMalloc(&sd.tw[k][i], f32.size() * 4)) != cudaSuccess) return bad(e, "cudaMalloc(split twiddles)");
-      if ((e = cudaMemcpy(sd.tw[k][i], f32.data(), f32.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
+      if (k == 2) {  // exact slices: the fixed-point engine's 60-bit limb twiddles
+        if (fx.empty()) fx.assign(4, 0);
+        src = fx.data();
+        bytes = fx.size() * 4;
+      } else {
+        for (size_t q = 0; q < f64.size(); ++q) f32[q] = (float)f64[q];
+        src = f32.data();
+        bytes = f32.size() * 4;
+      }
+      if ((e = cudaMalloc(&sd.tw[k][i], bytes)) != cudaSuccess) return bad(e, "cudaMalloc(split twiddles)");
+      if ((e = cudaMemcpy(sd.tw[k][i], src, bytes, cudaMemcpyHostToDevice)) != cudaSuccess)
         return bad(e, "cudaMemcpy(split twiddles)");
     }
   }
@@ -166,16 +211,18 @@ fftoc_status split_device(SplitDevice** out) {
 
 bool split_supported(int n, int kind) {
   const int idx = size_index(n);
-  return idx >= 0 && (kind == FFTOC_SPLIT_BF16X3 || kind == FFTOC_SPLIT_TF32X2) &&
-         host_split(kind == FFTOC_SPLIT_BF16X3 ? 0 : 1)[idx].fn != nullptr;
+  return idx >= 0 && kind >= FFTOC_SPLIT_BF16X3 && kind <= FFTOC_SPLIT_EXACT &&
+         host_split(kind_index(kind))[idx].fn != nullptr;
 }
 
 fftoc_status split_plan_info(int n, int kind, fftoc_plan_info* info) {
   if (!split_supported(n, kind)) return set_error(FFTOC_ERR_UNSUPPORTED, "no split-precision plan for this size");
-  const SplitDesc& d = host_split(kind == FFTOC_SPLIT_BF16X3 ? 0 : 1)[size_index(n)];
+  const SplitDesc& d = host_split(kind_index(kind))[size_index(n)];
   memset(info, 0, sizeof(*info));
   info->n = n;
-  info->engine = kind == FFTOC_SPLIT_BF16X3 ? FFTOC_ENGINE_SPLIT_BF16X3 : FFTOC_ENGINE_SPLIT_TF32X2;
+  info->engine = kind == FFTOC_SPLIT_BF16X3 ? FFTOC_ENGINE_SPLIT_BF16X3
+                 : kind == FFTOC_SPLIT_TF32X2 ? FFTOC_ENGINE_SPLIT_TF32X2
+                                              : FFTOC_ENGINE_SPLIT_EXACT;
   info->threads_per_transform = n / 16;
   info->transforms_per_block = d.tpb;
   info->threads_per_block = d.threads;
@@ -193,7 +240,7 @@ fftoc_status split_plan_info(int n, int kind, fftoc_plan_info* info) {
 fftoc_status launch_split(int n, const double* in, double* out, int64_t batch, int kind, cudaStream_t stream) {
   const int idx = size_index(n);
   if (idx < 0) return set_error(FFTOC_ERR_INVALID_SIZE, "n=" + std::to_string(n) + " is not one of 8,16,...,4096");
-  if (kind != FFTOC_SPLIT_BF16X3 && kind != FFTOC_SPLIT_TF32X2) return set_error(FFTOC_ERR_INVALID_VALUE, "unknown split kind");
+  if (kind < FFTOC_SPLIT_BF16X3 || kind > FFTOC_SPLIT_EXACT) return set_error(FFTOC_ERR_INVALID_VALUE, "unknown split kind");
   if (batch < 0) return set_error(FFTOC_ERR_INVALID_VALUE, "batch must be >= 0");
   if (!split_supported(n, kind)) return set_error(FFTOC_ERR_UNSUPPORTED, "no split-precision plan for n=" + std::to_string(n));
   if (batch == 0) return FFTOC_OK;
@@ -206,7 +253,7 @@ fftoc_status launch_split(int n, const double* in, double* out, int64_t batch, i
   SplitDevice* sd = nullptr;
   fftoc_status st = split_device(&sd);
   if (st != FFTOC_OK) return st;
-  const int k = kind == FFTOC_SPLIT_BF16X3 ? 0 : 1;
+  const int k = kind_index(kind);
   const SplitDesc& d = sd->d[k][idx];
   const long long tiles = (batch + d.tpb - 1) / d.tpb;
   const long long cap = (long long)sd->sms * d.blocks_per_sm;

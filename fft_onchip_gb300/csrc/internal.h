@@ -68,19 +68,22 @@ struct SplitDesc {
   int esize = 0, slices = 0;
   int blocks_per_sm = 0;
 };
-// kernels_split.cu; kind 1 = BF16x3, 2 = TF32x2
+// kernels_split.cu; kind 1 = BF16x3, 2 = TF32x2, 3 = exact slices
 void describe_split(int kind, SplitDesc* per_size);
 // api_split.cu; kind = fftoc_split_kind
 bool split_supported(int n, int kind);
 fftoc_status split_plan_info(int n, int kind, fftoc_plan_info* info);
 fftoc_status launch_split(int n, const double* in, double* out, int64_t batch, int kind, cudaStream_t stream);
 inline bool is_split_engine(int engine) {
-  return engine == FFTOC_ENGINE_SPLIT_BF16X3 || engine == FFTOC_ENGINE_SPLIT_TF32X2;
+  return engine == FFTOC_ENGINE_SPLIT_BF16X3 || engine == FFTOC_ENGINE_SPLIT_TF32X2 ||
+         engine == FFTOC_ENGINE_SPLIT_EXACT;
 }
 inline int split_kind_of(int engine) {
-  return engine == FFTOC_ENGINE_SPLIT_BF16X3 ? FFTOC_SPLIT_BF16X3 : FFTOC_SPLIT_TF32X2;
+  return engine == FFTOC_ENGINE_SPLIT_BF16X3   ? FFTOC_SPLIT_BF16X3
+         : engine == FFTOC_ENGINE_SPLIT_TF32X2 ? FFTOC_SPLIT_TF32X2
+                                               : FFTOC_SPLIT_EXACT;
 }
-constexpr int kLastEngine = FFTOC_ENGINE_SPLIT_TF32X2;
+constexpr int kLastEngine = FFTOC_ENGINE_SPLIT_EXACT;
 
 // Resident CTAs per SM of a persistent kernel, and the shared-memory carveout
 // that holds exactly that many (the rest of the SM's memory stays L1).  The

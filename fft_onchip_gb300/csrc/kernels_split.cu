@@ -1,7 +1,9 @@
 // fftoc — split-precision form instantiations: one plan per size (radix-16
 // GEMM passes, a radix 2/4/8 last pass where N is not a power of 16), for
-// BF16x3 and TF32x2 operand splits.  256 threads = two groups of 128
-// butterfly rows per CTA, two CTAs per SM.
+// the BF16x3 and TF32x2 operand splits (two CTAs per SM) and the exact-slice
+// form (fft_exact.cuh, one CTA per SM: its accumulators fill TMEM).  256
+// threads = two groups of 128 butterfly rows per CTA.
+#include "fft_exact.cuh"
 #include "fft_split.cuh"
 #include "internal.h"
 
@@ -37,11 +39,39 @@ void describe(SplitDesc* d) {
   add_split<KIND, PlanT<4096, 16, 1, 16, 16, 16, 1, 2>>(d[9]);
 }
 
+template <class PL>
+void add_exact(SplitDesc& d) {
+  using XP = ExactPlan<PL, 2>;
+  d.fn = (const void*)&fft_exact_kernel<PL, 2>;
+  d.threads = XP::THREADS;
+  d.tpb = PL::TPB;
+  d.smem = XP::SMEM;
+  d.passes = PL::S;
+  for (int i = 0; i < 4; ++i) d.radix[i] = PL::R[i];
+  d.tw_entries = PL::TW_COUNT;
+  d.b_bytes = XP::B_BYTES;
+  d.esize = 2;
+  d.slices = kExactDigits;
+}
+
+void describe_exact(SplitDesc* d) {
+  add_exact<PlanT<16, 16, 256, 16>>(d[1]);
+  add_exact<PlanT<32, 16, 128, 16, 2>>(d[2]);
+  add_exact<PlanT<64, 16, 64, 16, 4>>(d[3]);
+  add_exact<PlanT<128, 16, 32, 16, 8>>(d[4]);
+  add_exact<PlanT<256, 16, 16, 16, 16>>(d[5]);
+  add_exact<PlanT<512, 16, 8, 16, 16, 2>>(d[6]);
+  add_exact<PlanT<1024, 16, 4, 16, 16, 4>>(d[7]);
+  add_exact<PlanT<2048, 16, 2, 16, 16, 8>>(d[8]);
+  add_exact<PlanT<4096, 16, 1, 16, 16, 16>>(d[9]);
+}
+
 }  // namespace
 
 void describe_split(int kind, SplitDesc* per_size) {
   if (kind == kSplitBF16x3) describe<kSplitBF16x3>(per_size);
-  else describe<kSplitTF32x2>(per_size);
+  else if (kind == kSplitTF32x2) describe<kSplitTF32x2>(per_size);
+  else describe_exact(per_size);
 }
 
 }  // namespace fftoc

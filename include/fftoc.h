@@ -70,11 +70,14 @@ typedef enum {
   FFTOC_ENGINE_SPLIT_BF16X3 = 4, /* split-precision form, 3 BF16 terms per
                             operand on the tensor cores, FP32 accumulation and
                             data (relative L2 error ~1e-7; n >= 16)              */
-  FFTOC_ENGINE_SPLIT_TF32X2 = 5  /* split-precision form, 2 TF32 terms     */
+  FFTOC_ENGINE_SPLIT_TF32X2 = 5, /* split-precision form, 2 TF32 terms    */
+  FFTOC_ENGINE_SPLIT_EXACT = 6   /* exact-slice split form: block fixed point,
+                            six 8-bit digits per operand on the BF16 tensor
+                            cores, products exact in FP32 (error ~1e-14)    */
 } fftoc_engine;
 
 /* Operand splits of the split-precision form (fftoc_c2c_fwd_split). */
-typedef enum { FFTOC_SPLIT_BF16X3 = 1, FFTOC_SPLIT_TF32X2 = 2 } fftoc_split_kind;
+typedef enum { FFTOC_SPLIT_BF16X3 = 1, FFTOC_SPLIT_TF32X2 = 2, FFTOC_SPLIT_EXACT = 3 } fftoc_split_kind;
 
 typedef struct CUstream_st *fftoc_stream; /* same type as cudaStream_t */
 
@@ -106,7 +109,11 @@ fftoc_status fftoc_c2c_fwd_ex(int n, const double *in, double *out, int64_t batc
  * terms (FFTOC_SPLIT_TF32X2, three products), accumulated in FP32; data
  * between passes and the twiddle products are FP32; input and output are
  * binary64, with an exact power-of-two scale per transform when its largest
- * magnitude is outside [2^-60, 2^60].  Same arguments and conventions as
+ * magnitude is outside [2^-60, 2^60].  FFTOC_SPLIT_EXACT keeps the block
+ * fixed point of FFTOC_ENGINE_FX between passes and cuts each operand into
+ * six balanced 8-bit digits whose products, summed per slice order, are exact
+ * in FP32 (the 21 orders-0..5 products are kept), which meets the 1e-11 gate
+ * of the split form.  Same arguments and conventions as
  * fftoc_c2c_fwd; n = 16..4096 (FFTOC_ERR_UNSUPPORTED for n = 8).  Also
  * reachable as engines FFTOC_ENGINE_SPLIT_* of fftoc_c2c_fwd_ex. */
 fftoc_status fftoc_c2c_fwd_split(int n, const double *in, double *out, int64_t batch, int kind,

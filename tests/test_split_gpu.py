@@ -5,8 +5,10 @@ in place, and refusal of unsupported sizes.
 
 Tolerances (relative L2 error per batch, stated per split): BF16x3 carries
 FP32 data between passes and accumulates six BF16 term products in FP32,
-so its error is a few FP32 roundings per pass (measured ~1e-7); TF32x2 keeps
-two 11-bit terms (22 bits) per operand (measured ~1e-6)."""
+so its error is a few FP32 roundings per pass (measured 6e-7..9e-7); TF32x2
+keeps two 11-bit terms (22 bits) per operand (measured 6e-7..1e-6); the
+exact-slice form keeps 48-bit digits with products exact in FP32 and must
+meet the split form's 1e-11 gate."""
 import numpy as np
 import pytest
 
@@ -16,7 +18,7 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 SIZES = (16, 32, 64, 128, 256, 512, 1024, 2048, 4096)
-TOL = {"split_bf16x3": 1e-6, "split_tf32x2": 1e-5}
+TOL = {"split_bf16x3": 1e-6, "split_tf32x2": 1e-5, "split_exact": 1e-11}
 KINDS = tuple(TOL)
 
 
@@ -39,7 +41,8 @@ def test_split_matches_oracle(cuda, fftoc_lib, n, engine, family):
     ref = O.fft_f64(x)
     err = O.rel_l2(y, ref)
     assert err < TOL[engine], (n, engine, family, err)
-    assert err > 1e-12  # really the reduced-precision path, not binary64
+    if engine != "split_exact":
+        assert err > 1e-12  # really the reduced-precision path, not binary64
 
 
 @pytest.mark.parametrize("engine", KINDS)
@@ -75,11 +78,12 @@ def test_split_batch_edges_and_in_place(cuda, fftoc_lib, engine):
             assert np.array_equal(yi.view(np.uint64), y.view(np.uint64)), (n, batch)
 
 
-def test_split_zero_and_nonfinite(cuda, fftoc_lib):
+@pytest.mark.parametrize("engine", KINDS)
+def test_split_zero_and_nonfinite(cuda, fftoc_lib, engine):
     x = np.zeros((4, 256), dtype=np.complex128)
     x[2, 5] = np.nan
     x[3, 7] = np.inf
-    y = run(cuda, x, "split_bf16x3")
+    y = run(cuda, x, engine)
     assert np.all(y[0] == 0) and np.all(y[1] == 0)
     assert not np.all(np.isfinite(y[2])) and not np.all(np.isfinite(y[3]))
 
@@ -87,9 +91,10 @@ def test_split_zero_and_nonfinite(cuda, fftoc_lib):
 def test_split_refuses_n8_and_reports_plan(cuda, fftoc_lib):
     import fft_onchip_gb300 as F
     d = cuda.zeros(4, 8, dtype=cuda.complex128, device="cuda")
-    with pytest.raises(F.FftocError) as e:
-        F.fft(d, engine="split_bf16x3")
-    assert e.value.status_name == "FFTOC_ERR_UNSUPPORTED"
+    for eng in KINDS:
+        with pytest.raises(F.FftocError) as e:
+            F.fft(d, engine=eng)
+        assert e.value.status_name == "FFTOC_ERR_UNSUPPORTED"
     p = F.plan_query(4096, F.ENGINE_SPLIT_BF16X3)
     assert p["radix"] == [16, 16, 16] and p["threads_per_block"] == 256
     assert F.plan_query(512, F.ENGINE_SPLIT_TF32X2)["radix"] == [16, 16, 2]
