@@ -56,9 +56,9 @@ def parse():
     ap.add_argument("--gib", type=float, default=1.0, help="input GiB per size (1.0 = the sweep configuration)")
     ap.add_argument("--plan", default="", help="N:variant,... plan overrides (default: the library's choice)")
     ap.add_argument("--tuning", default="", help="tuning JSON written by fft_onchip_gb300.tune to apply")
-    ap.add_argument("--forms", default="split,uneven,serve,onchip",
-                    help="extra workloads measured after the sweep (comma list of: split, uneven, serve, onchip; "
-                         "empty for none)")
+    ap.add_argument("--forms", default="split,uneven,serve,onchip,cufft",
+                    help="extra workloads measured after the sweep (comma list of: split, uneven, serve, onchip, "
+                         "cufft; empty for none)")
     ap.add_argument("--serve-rates", default="1e3,1e4,1e5,1e6", help="offered request rates (req/s) of the serving loop")
     ap.add_argument("--uneven-count", type=int, default=200000)
     return ap.parse_args()
@@ -363,6 +363,8 @@ def run_ours(args, world, rank, local):
         forms["serve"] = bench_serve(args, torch, F)
     if "onchip" in args.forms.split(",") and rank == 0:
         forms["onchip"] = bench_onchip(args, torch, F)
+    if "cufft" in args.forms.split(","):
+        forms["cufft"] = bench_cufft(args, torch, sizes, bufs, stream, per_n)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -450,6 +452,32 @@ def bench_split(args, torch, F, dev, stream, world, per_n):
             row[name]["speedup_vs_f64_engine"] = round(row["f64"]["ms"] / row[name]["ms"], 3)
         out["per_n"][str(n)] = row
         del x, y
+    return out
+
+
+def bench_cufft(args, torch, sizes, bufs, stream, per_n):
+    """The device library on the same buffers: cuFFT's batched Z2Z forward
+    transform (through torch.fft.fft), the stand-in for the reference's
+    cuFFTDx path; CUDA events, 1 GiB per size, same algorithmic bytes."""
+    hbm, _ = peaks()
+    out = {"workload": "cuFFT Z2Z forward (torch.fft.fft) on the sweep's buffers", "per_n": {}}
+    K = max(3, args.steps)
+    for n in sizes:
+        x, _, batch = bufs[n]
+        for _ in range(3):
+            y = torch.fft.fft(x, dim=-1)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(K):
+            y = torch.fft.fft(x, dim=-1)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / K
+        gbs = 32.0 * n * batch / (ms * 1e-3) / 1e9
+        out["per_n"][str(n)] = {"ms": round(ms, 4), "hbm_gbs": round(gbs, 1), "frac_hbm": round(gbs / hbm, 4),
+                                "fftoc_speedup": round(per_n[str(n)]["hbm_gbs"] / gbs, 3)}
+        del y
     return out
 
 

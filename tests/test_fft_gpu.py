@@ -229,3 +229,18 @@ def test_full_size_properties(cuda, fftoc_lib, n):
     assert O.rel_l2(y[idx].cpu().numpy(), O.fft_f64(xs)) < TOL
     del x, y
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_matches_cufft(cuda, fftoc_lib, n):
+    """Device-library cross-check: cuFFT's batched Z2Z forward transform
+    (through torch.fft.fft), the stand-in for the reference's cuFFTDx path
+    (includes/reference.cuh:9-24), which is not available here."""
+    import fft_onchip_gb300 as F
+    x = inputs.normal(n, max(4, (1 << 16) // n), seed=n + 5)
+    d = cuda.from_numpy(x).cuda()
+    ours = F.fft(d).cpu().numpy()
+    cufft = cuda.fft.fft(d, dim=-1).cpu().numpy()
+    ref = O.fft_f64(x)
+    assert O.rel_l2(ours, cufft) < TOL
+    assert O.rel_l2(cufft, ref) < TOL
