@@ -314,6 +314,7 @@ fft_exact_kernel(const double2* __restrict__ in, double2* __restrict__ out, long
 
   const long long ntiles = (batch + TPB - 1) / TPB;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    if (c.tid == 0) prefetch_next_tile<N, TPB>(in, tile, batch);
     const long long tr = tile * TPB + c.j;
     const bool active = tr < batch;
     double2 raw[16];

@@ -128,6 +128,29 @@ __device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Bulk prefetch of [p, p + bytes) into L2 (no shared memory involved);
+// p 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// The next tile of a persistent CTA into L2 while it works on this one.
+template <int N, int TPB>
+__device__ __forceinline__ void prefetch_next_tile(const double2* in, long long tile, long long batch) {
+  const long long next = tile + gridDim.x;
+  const long long first = next * TPB;
+  if (first >= batch) return;
+  const long long count = batch - first < TPB ? batch - first : TPB;
+  const char* p = reinterpret_cast<const char*>(in + first * N);
+  long long bytes = count * N * 16;
+  while (bytes > 0) {  // in pieces of at most 64 KiB
+    const unsigned b = bytes > 65536 ? 65536u : (unsigned)bytes;
+    prefetch_l2(p, b);
+    p += b;
+    bytes -= b;
+  }
+}
+
 __device__ __forceinline__ unsigned tf32_rna(float x) {
   unsigned r;
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
@@ -431,6 +454,7 @@ fft_split_kernel(const double2* __restrict__ in, double2* __restrict__ out, long
 
   const long long ntiles = (batch + TPB - 1) / TPB;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    if (c.tid == 0) prefetch_next_tile<N, TPB>(in, tile, batch);
     const long long tr = tile * TPB + c.j;
     const bool active = tr < batch;
     // ---- load: point i of this thread is element t + T*i; per-transform
