@@ -229,8 +229,9 @@ def run_reference(args, world, rank):
 # GPU arm
 # ----------------------------------------------------------------------------
 def _plan_str(p):
-    return "%s%s P=%d tpb=%d" % ("persistent " if p.get("persistent") else "", "x".join(map(str, p["radix"])),
-                                 p["points_per_thread"], p["transforms_per_block"])
+    return "%s%s P=%d tpb=%d%s" % ("persistent " if p.get("persistent") else "", "x".join(map(str, p["radix"])),
+                                   p["points_per_thread"], p["transforms_per_block"],
+                                   " L2-prefetch" if p.get("prefetch") else "")
 
 
 def run_ours(args, world, rank, local):

@@ -101,6 +101,7 @@ class PlanInfo(ctypes.Structure):
         ("variants", ctypes.c_int),
         ("persistent", ctypes.c_int),
         ("stages", ctypes.c_int),
+        ("prefetch", ctypes.c_int),
     ]
 
 
@@ -214,6 +215,7 @@ def _info_dict(info):
         "variants": info.variants,
         "persistent": info.persistent,
         "stages": info.stages,
+        "prefetch": info.prefetch,
     }
 
 

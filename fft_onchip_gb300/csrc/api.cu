@@ -365,6 +365,7 @@ fftoc_status plan_query(int n, int engine, int variant, fftoc_plan_info* info) {
   info->variants = sv.count;
   info->persistent = d.persistent;
   info->stages = d.stages;
+  info->prefetch = d.prefetch;
   return FFTOC_OK;
 }
 

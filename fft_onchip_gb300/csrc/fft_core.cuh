@@ -38,6 +38,7 @@ struct PlanT {
   static constexpr int P = P_;
   static constexpr int TPB = TPB_;
   static constexpr int MINB = MINB_;  // minimum resident CTAs per SM (register budget)
+  static constexpr bool PREFETCH = false;  // batched kernel: L2 prefetch one wave ahead (Prefetched<>)
   static constexpr int R[4] = {R0, R1, R2, R3};
   static constexpr int S = (R0 > 1) + (R1 > 1) + (R2 > 1) + (R3 > 1);
   static constexpr int T = N / P;
@@ -187,6 +188,13 @@ template <> struct Konst<EngFx> {
   FFTOC_HD static EngFx::KC s8() { return {410903206, 732584116}; }
   FFTOC_HD static EngFx::KC nc8() { return {-992008095, 649682156}; }
   FFTOC_HD static EngFx::KC ns8() { return {-410903207, 341157708}; }
+};
+
+// A plan whose batched kernel also prefetches, into L2, the tile of the CTA
+// that starts one full wave (SMs x MINB CTAs) later.
+template <class PL>
+struct Prefetched : PL {
+  static constexpr bool PREFETCH = true;
 };
 
 // ---------------------------------------------------------------------------

@@ -431,6 +431,26 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
   extern __shared__ __align__(16) unsigned char smem_raw[];
   longlong2* sm = reinterpret_cast<longlong2*>(smem_raw);
 
+  if constexpr (PL::PREFETCH) {
+    if (threadIdx.x == 0) {
+      // the tile of the CTA that starts one full wave later, into L2
+      unsigned nsm;
+      asm("mov.u32 %0, %%nsmid;" : "=r"(nsm));
+      const long long first = ((long long)blockIdx.x + (long long)nsm * PL::MINB) * TPB;
+      if (first < batch) {
+        const long long cnt = batch - first < TPB ? batch - first : TPB;
+        const char* p = reinterpret_cast<const char*>(in + first * N);
+        long long bytes = cnt * N * 16;
+        while (bytes > 0) {  // pieces of at most 64 KiB; 16-byte aligned multiples of 16
+          const unsigned b = bytes > 65536 ? 65536u : (unsigned)bytes;
+          asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(b) : "memory");
+          p += b;
+          bytes -= b;
+        }
+      }
+    }
+  }
+
   const int tid = threadIdx.x;
   const int j = tid / T;
   const int t = tid - j * T;

@@ -32,6 +32,7 @@ struct KernelDesc {
   int persistent = 0;        // 1: grid-stride persistent CTAs with TMA prefetch (extra error-flag argument)
   int stages = 0;            // shared-memory stages of the persistent kernel
   int blocks_per_sm = 0;     // resident CTAs per SM (filled at device set-up)
+  int prefetch = 0;          // 1: L2 prefetch one wave ahead (Prefetched<> plans)
   // uneven-batch kernel of the same plan (nullptr for TMA-prefetching plans)
   const void* fn_uneven = nullptr;
   int smem_uneven = 0;

@@ -67,9 +67,9 @@ def tune(sizes=SIZES, engines=("fx", "f64"), gib=0.5, apply=True, verbose=True):
             if verbose:
                 for v, ms, p in res:
                     gbs = 32.0 * n * (int(gib * (1 << 30)) // (16 * n)) / (ms * 1e-3) / 1e9
-                    print("%-4s N=%-5d variant %d radix=%-14s P=%-2d tpb=%-3d %8.4f ms %7.1f GB/s%s" % (
+                    print("%-4s N=%-5d variant %d radix=%-14s P=%-2d tpb=%-3d%s %8.4f ms %7.1f GB/s%s" % (
                         eng, n, v, "x".join(map(str, p["radix"])), p["points_per_thread"], p["transforms_per_block"],
-                        ms, gbs, "  <- best" if v == best[0] else ""))
+                        " pf" if p.get("prefetch") else "   ", ms, gbs, "  <- best" if v == best[0] else ""))
     return {"gpu": gpu, "choices": table}
 
 

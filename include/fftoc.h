@@ -167,6 +167,8 @@ typedef struct {
   int variants;               /* number of compiled plans for (n, engine)    */
   int persistent;             /* 1: persistent CTAs, TMA-prefetched tiles    */
   int stages;                 /* shared-memory stages (persistent plans)     */
+  int prefetch;               /* 1: each CTA prefetches, into L2, the tile of
+                                 the CTA one full wave later                 */
 } fftoc_plan_info;
 
 /* Plan currently used for (n, engine). */
