@@ -62,6 +62,7 @@ EXPORTS = tuple(["fftoc_c2c_fwd_n%d" % n for n in SIZES]) + (
     "fftoc_server_destroy",
     "fftoc_onchip_plan",
     "fftoc_onchip_run",
+    "fftoc_selftest_bounded_wait",
 )
 
 
@@ -189,6 +190,8 @@ def load(path=None):
     L.fftoc_onchip_plan.restype = c_int
     L.fftoc_onchip_run.argtypes = [c_int, c_int, vp, i64, c_int, vp]
     L.fftoc_onchip_run.restype = c_int
+    L.fftoc_selftest_bounded_wait.argtypes = [ctypes.c_double, vp]
+    L.fftoc_selftest_bounded_wait.restype = c_int
     _lib = L
     return L
 

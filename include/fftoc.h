@@ -325,6 +325,14 @@ fftoc_status fftoc_onchip_run(int n, int engine, double *data, int64_t blocks, i
  * otherwise.  Clears the flag.  Synchronous. */
 fftoc_status fftoc_device_error_check(void);
 
+/* Self-test of the failure path of the bounded device waits: one CTA waits
+ * on an mbarrier that nothing arrives on, gives up after limit_ms (0 < limit_ms
+ * <= 1000), raises the device error flag and returns; a following
+ * fftoc_device_error_check() reports FFTOC_ERR_TIMEOUT.  Asynchronous on
+ * `stream`.  (The persistent, split and exact kernels take the same path when
+ * a wait for a copy or an MMA does not complete in 2 s.) */
+fftoc_status fftoc_selftest_bounded_wait(double limit_ms, fftoc_stream stream);
+
 /* Engine that FFTOC_ENGINE_AUTO resolves to for size n. */
 int fftoc_auto_engine(int n);
 
