@@ -270,6 +270,19 @@ __device__ __forceinline__ void dft_small(float (&re)[16], float (&im)[16], int 
   }
 }
 
+// Multiply this thread's stored outputs by 2^unshift (exact, binary64).
+template <int T, int R, int Bq, int p>
+__device__ __noinline__ void split_unscale_outputs(double2* dst, int t, int unshift) {
+  for (int b = 0; b < Bq; ++b)
+    for (int m = 0; m < R; ++m) {
+      const int tp = t + T * b;
+      const int k = tp & (p - 1);
+      double2* q = dst + (tp - k) * R + k + m * p;
+      const double2 v = *q;
+      *q = make_double2(ldexp(v.x, unshift), ldexp(v.y, unshift));
+    }
+}
+
 // Per-CTA state shared by the passes.
 struct SplitCtx {
   unsigned char* sA;
@@ -401,8 +414,11 @@ __device__ __forceinline__ void split_pass(SplitCtx& c, float (&re)[16], float (
           const int tp = c.t + T * b;
           const int k = tp & (p - 1);
           const double xr = f32_to_f64_int(re[b + Bq * m]), xi = f32_to_f64_int(im[b + Bq * m]);
-          dst[(tp - k) * R + k + m * p] = scaled ? make_double2(ldexp(xr, unshift), ldexp(xi, unshift)) : make_double2(xr, xi);
+          dst[(tp - k) * R + k + m * p] = make_double2(xr, xi);
         }
+      // rare transforms scaled at the input: undo the scale in place, out of
+      // line (an if-converted ldexp would occupy the FP64 pipe for every value)
+      if (scaled) split_unscale_outputs<T, R, Bq, p>(dst, c.t, unshift);
     }
   }
 }
