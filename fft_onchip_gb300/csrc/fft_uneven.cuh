@@ -155,6 +155,12 @@ fft_uneven_kernel(const UnevenArgs* __restrict__ a, int bin, const typename E::T
     if (threadIdx.x < TPB) {
       const long long k = tile0 + threadIdx.x;
       base[threadIdx.x] = k < count ? __ldg(offsets + __ldg(list + k)) : 0;
+      // this CTA's next tile, transform by transform, into L2
+      const long long kn = k + (long long)gridDim.x * TPB;
+      if (kn < count) {
+        const double2* q = a->in + __ldg(offsets + __ldg(list + kn));
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(q), "r"((unsigned)(PL::N * 16)) : "memory");
+      }
     }
     __syncthreads();
     IndexedTile tl = proto;
