@@ -39,6 +39,7 @@ struct PlanT {
   static constexpr int TPB = TPB_;
   static constexpr int MINB = MINB_;  // minimum resident CTAs per SM (register budget)
   static constexpr bool PREFETCH = false;  // batched kernel: L2 prefetch one wave ahead (Prefetched<>)
+  static constexpr bool OUTLINE_SLOW_IN = false;  // batched kernel: rare input path out of line (OutlinedSlowIn<>)
   static constexpr int R[4] = {R0, R1, R2, R3};
   static constexpr int S = (R0 > 1) + (R1 > 1) + (R2 > 1) + (R3 > 1);
   static constexpr int T = N / P;
@@ -195,6 +196,14 @@ template <> struct Konst<EngFx> {
 template <class PL>
 struct Prefetched : PL {
   static constexpr bool PREFETCH = true;
+};
+
+// A plan whose batched kernel converts the rare transforms that leave the
+// fast binary64 -> fixed-point input path through an out-of-line function
+// (otherwise the compiler may if-convert that path into the fast one).
+template <class PL>
+struct OutlinedSlowIn : PL {
+  static constexpr bool OUTLINE_SLOW_IN = true;
 };
 
 // ---------------------------------------------------------------------------

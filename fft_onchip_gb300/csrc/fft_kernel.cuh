@@ -77,6 +77,13 @@ __device__ __noinline__ double fx_out_slow(long long x, int K) { return ldexp((d
 inline double fx_out_slow(long long x, int K) { return ldexp((double)x, K); }
 #endif
 
+// fx_in out of line, for the rare transforms that leave the fast input path.
+#ifdef __CUDA_ARCH__
+__device__ __noinline__ long long fx_in_slow(unsigned hw, unsigned lw, int eref) { return fx_in(hw, lw, eref); }
+#else
+inline long long fx_in_slow(unsigned hw, unsigned lw, int eref) { return fx_in(hw, lw, eref); }
+#endif
+
 // Scale parameters of a transform from its largest biased exponent.
 struct FxScale {
   int eref, K, kshift;
@@ -113,7 +120,8 @@ FFTOC_HD long long fx_in_near(unsigned hw, unsigned lw, int eref) {
 
 // Convert a thread's P raw points; the fast path is taken when every value is
 // normal and within 2^31 of the transform maximum (the usual case).
-template <int P>
+// OUTLINE: the other path calls the out-of-line fx_in_slow.
+template <int P, bool OUTLINE = false>
 FFTOC_HD void fx_convert_in(const double2 (&raw)[P], long long (&re)[P], long long (&im)[P], int eref) {
   int emin = 0x7FF;
 #pragma unroll
@@ -127,6 +135,12 @@ FFTOC_HD void fx_convert_in(const double2 (&raw)[P], long long (&re)[P], long lo
     for (int i = 0; i < P; ++i) {
       re[i] = fx_in_near(hi_word(raw[i].x), lo_word(raw[i].x), eref);
       im[i] = fx_in_near(hi_word(raw[i].y), lo_word(raw[i].y), eref);
+    }
+  } else if constexpr (OUTLINE) {
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      re[i] = fx_in_slow(hi_word(raw[i].x), lo_word(raw[i].x), eref);
+      im[i] = fx_in_slow(hi_word(raw[i].y), lo_word(raw[i].y), eref);
     }
   } else {
 #pragma unroll
@@ -511,7 +525,7 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
     K = sc.K;
     kshift = sc.kshift;
     slow = sc.slow;
-    fx_convert_in<P>(raw, re, im, sc.eref);
+    fx_convert_in<P, PL::OUTLINE_SLOW_IN>(raw, re, im, sc.eref);
   }
 
   if constexpr (F::STAGED) __syncthreads();  // staging buffer is reused by the passes
