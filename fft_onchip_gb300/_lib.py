@@ -63,6 +63,7 @@ EXPORTS = tuple(["fftoc_c2c_fwd_n%d" % n for n in SIZES]) + (
     "fftoc_onchip_plan",
     "fftoc_onchip_run",
     "fftoc_selftest_bounded_wait",
+    "fftoc_exec_twiddles",
 )
 
 
@@ -192,6 +193,8 @@ def load(path=None):
     L.fftoc_onchip_run.restype = c_int
     L.fftoc_selftest_bounded_wait.argtypes = [ctypes.c_double, vp]
     L.fftoc_selftest_bounded_wait.restype = c_int
+    L.fftoc_exec_twiddles.argtypes = [c_int, c_int, ctypes.POINTER(c_int), ctypes.POINTER(vp)]
+    L.fftoc_exec_twiddles.restype = c_int
     _lib = L
     return L
 

@@ -318,6 +318,16 @@ fftoc_status fftoc_server_destroy(fftoc_server server);
 fftoc_status fftoc_onchip_plan(int n, int engine, int *transforms_per_block, int *variant);
 fftoc_status fftoc_onchip_run(int n, int engine, double *data, int64_t blocks, int repeats, fftoc_stream stream);
 
+/* Twiddle table for the device-side executors of <fftoc/exec.cuh> (the
+ * FFTExec shape of includes/tensor_fft_64.cuh:12-45): the table of a plan of
+ * size n whose passes have radices radix[0..3] (each 2, 4, 8 or 16, unused
+ * passes 1 at the end), in the engine's layout (16 bytes per entry: binary64
+ * (cos, -sin), or fixed-point limbs), in device memory of the current device
+ * owned by the library until the process exits.  *table is NULL for a
+ * one-pass plan (no twiddles).  Engines: binary64, fixed point (AUTO
+ * resolves to the latter).  Synchronous on first use of a plan. */
+fftoc_status fftoc_exec_twiddles(int n, int engine, const int radix[4], const void **table);
+
 /* Device-side error flag of the current device: FFTOC_ERR_TIMEOUT if a
  * persistent kernel's bounded wait for a prefetched tile gave up since the
  * last check (its outputs are then incomplete), FFTOC_ERR_INVALID_VALUE if an
