@@ -165,28 +165,47 @@ def barrier(world):
 # ----------------------------------------------------------------------------
 # CPU baseline: the oracle's FP64 Stockham port on all host cores
 # ----------------------------------------------------------------------------
+def _timed(fn, x, seconds):
+    """(transforms, seconds) of repeated fn(x) for at least `seconds`."""
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        fn(x)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            return reps * x.shape[0], el
+
+
 def cpu_sample_rate(sizes, seconds_per_size):
+    """The port on all host threads (the baseline), plus two secondary points
+    on the same samples: the port on one thread and numpy.fft (pocketfft,
+    one thread).  Each is FFT/s over the sweep (transforms / summed time)."""
+    import numpy as np
     from fft_onchip_gb300 import inputs
     from oracle import oracle as O
     threads = O.max_threads()
-    total_ffts, total_t, per = 0, 0.0, {}
+    legs = {"all": (lambda x: O.fft_f64(x, threads=0), seconds_per_size),
+            "one": (lambda x: O.fft_f64(x, threads=1), seconds_per_size / 3),
+            "numpy": (lambda x: np.fft.fft(x, axis=1), seconds_per_size / 3)}
+    acc = {k: [0, 0.0, {}] for k in legs}
     for n in sizes:
         batch = (GIB // (16 * n))
         sample = max(1, batch // 64)
         x = inputs.normal(n, sample, seed=n)
         O.fft_f64(x[: max(1, sample // 16)], threads=0)  # warm the pool and caches
-        t0 = time.perf_counter()
-        reps = 0
-        while True:
-            O.fft_f64(x, threads=0)
-            reps += 1
-            el = time.perf_counter() - t0
-            if el >= seconds_per_size:
-                break
-        total_ffts += reps * sample
-        total_t += el
-        per[str(n)] = reps * sample / el
-    return total_ffts / total_t, threads, per
+        for k, (fn, sec) in legs.items():
+            f, el = _timed(fn, x, sec)
+            acc[k][0] += f
+            acc[k][1] += el
+            acc[k][2][str(n)] = f / el
+    rate = {k: v[0] / v[1] for k, v in acc.items()}
+    return rate["all"], threads, acc["all"][2], {
+        "nproc": os.cpu_count(),
+        "one_core": {"value": rate["one"], "cores": 1,
+                     "per_n": {k: round(v, 1) for k, v in acc["one"][2].items()}},
+        "numpy_fft": {"value": rate["numpy"], "cores": 1, "what": "numpy.fft.fft (pocketfft) on the same samples",
+                      "per_n": {k: round(v, 1) for k, v in acc["numpy"][2].items()}}}
 
 
 def run_reference(args, world, rank):
@@ -369,10 +388,11 @@ def run_ours(args, world, rank, local):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        v, cores, per = cpu_sample_rate(sizes, args.cpu_seconds)
+        v, cores, per, extra = cpu_sample_rate(sizes, args.cpu_seconds)
         cpu = {"value": v, "unit": "FFT/s", "cores": cores, "kind": "port",
                "sample": "oracle FP64 Stockham (radix-8/4/2) on 1/64 of each size's batch, >= %.1f s per size"
                          % args.cpu_seconds, "per_n": {k: round(val, 1) for k, val in per.items()}}
+        cpu.update(extra)
 
     if rank == 0:
         resolved = sorted({F.plan_query(n, eng)["engine"] for n in sizes})
