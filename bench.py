@@ -248,9 +248,11 @@ def run_reference(args, world, rank):
 # GPU arm
 # ----------------------------------------------------------------------------
 def _plan_str(p):
-    return "%s%s P=%d tpb=%d%s" % ("persistent " if p.get("persistent") else "", "x".join(map(str, p["radix"])),
-                                   p["points_per_thread"], p["transforms_per_block"],
-                                   " L2-prefetch" if p.get("prefetch") else "")
+    from fft_onchip_gb300.tune import code_str
+    return "%s%s P=%d tpb=%d%s%s" % ("persistent " if p.get("persistent") else "", "x".join(map(str, p["radix"])),
+                                     p["points_per_thread"], p["transforms_per_block"],
+                                     " L2-prefetch" if p.get("prefetch") else "",
+                                     (" " + code_str(p)) if p.get("code_flags") else "")
 
 
 def run_ours(args, world, rank, local):

@@ -104,6 +104,7 @@ class PlanInfo(ctypes.Structure):
         ("persistent", ctypes.c_int),
         ("stages", ctypes.c_int),
         ("prefetch", ctypes.c_int),
+        ("code_flags", ctypes.c_int),
     ]
 
 
@@ -222,6 +223,7 @@ def _info_dict(info):
         "persistent": info.persistent,
         "stages": info.stages,
         "prefetch": info.prefetch,
+        "code_flags": info.code_flags,
     }
 
 

@@ -366,6 +366,7 @@ fftoc_status plan_query(int n, int engine, int variant, fftoc_plan_info* info) {
   info->persistent = d.persistent;
   info->stages = d.stages;
   info->prefetch = d.prefetch;
+  info->code_flags = d.code_flags;
   return FFTOC_OK;
 }
 

@@ -18,6 +18,7 @@
 //            integer adds, and products use 30-bit limbs on IMAD.WIDE.  The
 //            conversion back to binary64 rounds once (cvt.rn.f64.s64).
 #pragma once
+#include <type_traits>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -40,6 +41,8 @@ struct PlanT {
   static constexpr int MINB = MINB_;  // minimum resident CTAs per SM (register budget)
   static constexpr bool PREFETCH = false;  // batched kernel: L2 prefetch one wave ahead (Prefetched<>)
   static constexpr bool OUTLINE_SLOW_IN = false;  // batched kernel: rare input path out of line (OutlinedSlowIn<>)
+  static constexpr bool IMAD_SPLIT = false;  // fixed point: low limbs by integer multiply-add (ImadSplit<>)
+  static constexpr bool OUT_HI_ZERO = false;  // fixed point: zero test on the converted word (OutHiZero<>)
   static constexpr int R[4] = {R0, R1, R2, R3};
   static constexpr int S = (R0 > 1) + (R1 > 1) + (R2 > 1) + (R3 > 1);
   static constexpr int T = N / P;
@@ -91,10 +94,19 @@ struct EngF64 {
   }
 };
 
-struct EngFx {
+// Limbs of a fixed-point constant: v*2^60 = h*2^30 + l, 0 <= l < 2^30.
+struct FxKC {
+  int h, l;
+};
+
+// IMAD_SPLIT selects how the low limb of a split is formed (a logic op or an
+// integer multiply-add: same value, different pipe); the plans choose the form
+// that measured faster.
+template <bool IMAD_SPLIT = false>
+struct EngFxT {
   using S = long long;
   using TW = int4;      // (wr.h, wr.l, wi.h, wi.l): w*2^60 = h*2^30 + l, 0 <= l < 2^30
-  struct KC { int h, l; };
+  using KC = FxKC;
   static constexpr int kId = 2;
   FFTOC_HD static S add(S a, S b) { return a + b; }
   FFTOC_HD static S sub(S a, S b) { return a - b; }
@@ -130,6 +142,12 @@ struct EngFx {
   // Limbs of a value, |x| < 2^61: x = xh*2^30 + xl, |xh| < 2^31, 0 <= xl < 2^30.
   FFTOC_HD static void split(S x, int& xh, int& xl) {
     xh = (int)(x >> 30);
+#ifdef __CUDA_ARCH__
+    if constexpr (IMAD_SPLIT) {  // lo32(x) - xh * 2^30 (mod 2^32)
+      asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(xl) : "r"(xh), "r"(0xC0000000u), "r"((unsigned)x));
+      return;
+    }
+#endif
     xl = (int)((unsigned)x & 0x3FFFFFFFu);
   }
   // a*b + c with a, b 32-bit and c 64-bit: one IMAD.WIDE (spelled out in PTX;
@@ -169,6 +187,7 @@ struct EngFx {
   FFTOC_HD static void cmul(S& xr, S& xi, const int4 w) { cmul_limbs(xr, xi, w.x, w.y, w.z, w.w); }
   FFTOC_HD static void cmulk(S& xr, S& xi, KC c, KC s) { cmul_limbs(xr, xi, c.h, c.l, s.h, s.l); }
 };
+using EngFx = EngFxT<false>;
 
 // constants of the DFT kernels, per engine
 template <class E> struct Konst;
@@ -182,13 +201,13 @@ template <> struct Konst<EngF64> {
   FFTOC_HD static EngF64::KC ns8() { return {-0.38268343236508977173}; }
 };
 // Fixed-point limbs of the same constants: v*2^60 = h*2^30 + l, 0 <= l < 2^30.
-template <> struct Konst<EngFx> {
-  FFTOC_HD static EngFx::KC h() { return {759250124, 1067312712}; }
-  FFTOC_HD static EngFx::KC nh() { return {-759250125, 6429112}; }
-  FFTOC_HD static EngFx::KC c8() { return {992008094, 424059668}; }
-  FFTOC_HD static EngFx::KC s8() { return {410903206, 732584116}; }
-  FFTOC_HD static EngFx::KC nc8() { return {-992008095, 649682156}; }
-  FFTOC_HD static EngFx::KC ns8() { return {-410903207, 341157708}; }
+template <bool B> struct Konst<EngFxT<B>> {
+  FFTOC_HD static FxKC h() { return {759250124, 1067312712}; }
+  FFTOC_HD static FxKC nh() { return {-759250125, 6429112}; }
+  FFTOC_HD static FxKC c8() { return {992008094, 424059668}; }
+  FFTOC_HD static FxKC s8() { return {410903206, 732584116}; }
+  FFTOC_HD static FxKC nc8() { return {-992008095, 649682156}; }
+  FFTOC_HD static FxKC ns8() { return {-410903207, 341157708}; }
 };
 
 // A plan whose batched kernel also prefetches, into L2, the tile of the CTA
@@ -205,6 +224,25 @@ template <class PL>
 struct OutlinedSlowIn : PL {
   static constexpr bool OUTLINE_SLOW_IN = true;
 };
+
+// A plan whose fixed-point splits form the low limb with an integer
+// multiply-add instead of a mask (moves work from the ALU pipe to the FMA pipe).
+template <class PL>
+struct ImadSplit : PL {
+  static constexpr bool IMAD_SPLIT = true;
+};
+
+// A plan whose output conversion tests the converted value's high word for
+// zero instead of the 64-bit integer (one compare less per value).
+template <class PL>
+struct OutHiZero : PL {
+  static constexpr bool OUT_HI_ZERO = true;
+};
+
+// The engine a plan's kernels compute with: the fixed-point engine in the
+// plan's split form, or E unchanged.
+template <class E, class PL>
+using PlanEngine = typename std::conditional<E::kId == EngFx::kId && PL::IMAD_SPLIT, EngFxT<true>, E>::type;
 
 // ---------------------------------------------------------------------------
 // Small forward DFTs on registers.  re[i], im[i] at compile-time indices

@@ -62,10 +62,14 @@ FFTOC_HD long long fx_in(unsigned hw, unsigned lw, int eref) {
 // x * 2^K, K = Emax - 1022 - B: the correctly rounded conversion with K added
 // to its exponent field (exact).  Valid while every result exponent stays in
 // the normal range (fx_scale's `slow` is false); one FP64-pipe instruction.
+// HI_ZERO: test the converted high word for zero (a nonzero integer converts
+// to a normal number, so the two tests agree).
+template <bool HI_ZERO = false>
 FFTOC_HD double fx_out(long long x, int kshift) {
   const double d = (double)x;
   const unsigned hi = hi_word(d);
-  return from_words(x != 0 ? hi + (unsigned)kshift : hi, lo_word(d));
+  const bool nonzero = HI_ZERO ? hi != 0u : x != 0;
+  return from_words(nonzero ? hi + (unsigned)kshift : hi, lo_word(d));
 }
 
 // Transforms whose outputs may be subnormal or overflow: ldexp.  Kept out of
@@ -303,8 +307,9 @@ struct SmemTile {
 template <class E, class PL, class Tile>
 __device__ __forceinline__ void fft_tile(const Tile& tl, const typename E::TW* __restrict__ tw,
                                          unsigned char* smem_raw) {
-  using F = Fft<E, PL>;
-  using S = typename E::S;
+  using EK = PlanEngine<E, PL>;
+  using F = Fft<EK, PL>;
+  using S = typename EK::S;
   constexpr int N = PL::N, TPB = PL::TPB;
   constexpr int P = F::P, T = F::T, NS = F::NS;
   longlong2* sm = reinterpret_cast<longlong2*>(smem_raw);
@@ -381,7 +386,8 @@ __device__ __forceinline__ void fft_tile(const Tile& tl, const typename E::TW* _
       return make_double2(re[i], im[i]);
     } else {
       if (slow_bits) return make_double2(__longlong_as_double(re[i]), __longlong_as_double(im[i]));
-      return make_double2(fx_out((long long)re[i], kshift), fx_out((long long)im[i], kshift));
+      return make_double2(fx_out<PL::OUT_HI_ZERO>((long long)re[i], kshift),
+                          fx_out<PL::OUT_HI_ZERO>((long long)im[i], kshift));
     }
   };
   if constexpr (E::kId == EngFx::kId) {
@@ -438,8 +444,9 @@ __global__ void __launch_bounds__(Fft<E, PL>::THREADS, PL::MINB)
 fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long long batch,
                const typename E::TW* __restrict__ tw, int* __restrict__ err) {
   (void)err;  // no waits in this kernel; the argument keeps one launch signature
-  using F = Fft<E, PL>;
-  using S = typename E::S;
+  using EK = PlanEngine<E, PL>;
+  using F = Fft<EK, PL>;
+  using S = typename EK::S;
   constexpr int N = PL::N, TPB = PL::TPB;
   constexpr int P = F::P, T = F::T, NS = F::NS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -539,7 +546,8 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
       return make_double2(re[i], im[i]);
     } else {
       if (slow_bits) return make_double2(__longlong_as_double(re[i]), __longlong_as_double(im[i]));
-      return make_double2(fx_out((long long)re[i], kshift), fx_out((long long)im[i], kshift));
+      return make_double2(fx_out<PL::OUT_HI_ZERO>((long long)re[i], kshift),
+                          fx_out<PL::OUT_HI_ZERO>((long long)im[i], kshift));
     }
   };
   if constexpr (E::kId == EngFx::kId) {

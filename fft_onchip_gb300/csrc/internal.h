@@ -33,6 +33,7 @@ struct KernelDesc {
   int stages = 0;            // shared-memory stages of the persistent kernel
   int blocks_per_sm = 0;     // resident CTAs per SM (filled at device set-up)
   int prefetch = 0;          // 1: L2 prefetch one wave ahead (Prefetched<> plans)
+  int code_flags = 0;        // FFTOC_CODE_* bits of the plan
   // uneven-batch kernel of the same plan (nullptr for TMA-prefetching plans)
   const void* fn_uneven = nullptr;
   int smem_uneven = 0;

@@ -19,6 +19,12 @@ from . import _lib
 SIZES = _lib.SIZES
 
 
+def code_str(p):
+    """The code-form flags of a plan, e.g. 'outlined-in,imad-split'."""
+    names = ((1, "outlined-in"), (2, "imad-split"), (4, "out-hi-zero"))
+    return ",".join(nm for bit, nm in names if p.get("code_flags", 0) & bit)
+
+
 def time_variants(n, engine, gib=0.5, reps=20, warmup=5, device=0, rounds=2):
     """[(variant, ms per launch, plan dict)] for every compiled plan."""
     import torch
@@ -69,7 +75,8 @@ def tune(sizes=SIZES, engines=("fx", "f64"), gib=0.5, apply=True, verbose=True):
                     gbs = 32.0 * n * (int(gib * (1 << 30)) // (16 * n)) / (ms * 1e-3) / 1e9
                     print("%-4s N=%-5d variant %d radix=%-14s P=%-2d tpb=%-3d%s %8.4f ms %7.1f GB/s%s" % (
                         eng, n, v, "x".join(map(str, p["radix"])), p["points_per_thread"], p["transforms_per_block"],
-                        " pf" if p.get("prefetch") else "   ", ms, gbs, "  <- best" if v == best[0] else ""))
+                        " pf" if p.get("prefetch") else "   ", ms, gbs, "  <- best" if v == best[0] else "")
+                      + (" [%s]" % code_str(p) if p.get("code_flags") else ""))
     return {"gpu": gpu, "choices": table}
 
 
