@@ -337,6 +337,8 @@ def run_ours(args, world, rank, local):
     traffic = tt.get("fx" if dom_plan["engine"] == F.ENGINE_FX else "f64")
     if tt.get("plan") != _plan_str(dom_plan):
         traffic = None
+    elif traffic is not None:  # the table holds a 1 GiB launch; scale to this launch's transforms
+        traffic = int(round(traffic * bufs[dom][2] / (GIB // (16 * dom))))
     roofline = {"bound": "hbm", "achieved": round(dom_gbs, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(dom_gbs / hbm, 4), "traffic": traffic,
                 "kernel": "N=%d %s plan %s" % (dom, "fx" if F.plan_query(dom, eng)["engine"] == F.ENGINE_FX else "f64",
