@@ -21,7 +21,7 @@ struct fftoc_uneven_plan_s {
   int64_t max_count = 0;
   int chunks = 0;
   fftoc::UnevenArgs* args = nullptr;
-  int* list = nullptr;
+  long long* list = nullptr;  // bucketed transform offsets
   int* chunk_base = nullptr;
   int* err = nullptr;
   int sms = 0;
@@ -240,7 +240,7 @@ fftoc_status plan_create(fftoc_uneven_plan* out, int64_t max_count, int engine) 
     return s;
   };
   if ((e = cudaMalloc(&p->args, sizeof(UnevenArgs))) != cudaSuccess) return bad(cuda_err(e, "cudaMalloc(uneven args)"));
-  if ((e = cudaMalloc(&p->list, (size_t)max_count * sizeof(int))) != cudaSuccess)
+  if ((e = cudaMalloc(&p->list, (size_t)max_count * sizeof(long long))) != cudaSuccess)
     return bad(cuda_err(e, "cudaMalloc(uneven list)"));
   if ((e = cudaMalloc(&p->chunk_base, (size_t)p->chunks * kUnevenBins * sizeof(int))) != cudaSuccess)
     return bad(cuda_err(e, "cudaMalloc(uneven chunk table)"));

@@ -7,7 +7,7 @@
 // Here one graph takes the whole mixed batch:
 //   1. uneven_hist     per 1024-entry chunk of the table, a histogram by size;
 //   2. uneven_scan     bucket starts and per-chunk bases (one CTA);
-//   3. uneven_scatter  stable bucketing: transform indices grouped by size, in
+//   3. uneven_scatter  stable bucketing: transform offsets grouped by size, in
 //                      table order within a size;
 //   4. fft_uneven_kernel<E, PL>, one per size on parallel graph branches:
 //      persistent CTAs walk their size's bucket tile by tile, loading each
@@ -32,7 +32,7 @@ struct UnevenArgs {
   const long long* offsets;   // complex-element offset of each transform (in and out)
   const int* ns;              // size of each transform
   long long count;            // transforms in the table
-  int* list;                  // bucketed transform indices [max_count]
+  long long* list;            // bucketed transform offsets [max_count]
   int* chunk_base;            // [chunks][kUnevenBins]
   int bucket_count[kUnevenBins];
   int bucket_start[kUnevenBins];
@@ -106,8 +106,9 @@ static __global__ void __launch_bounds__(32 * kUnevenBins) uneven_scan(UnevenArg
   }
 }
 
-// Stable scatter: entry i goes to list[start(bin) + chunk base + rank of i
-// among the entries of its bin earlier in the chunk].
+// Stable scatter: the offset of entry i goes to list[start(bin) + chunk base +
+// rank of i among the entries of its bin earlier in the chunk], so the size
+// kernels find each transform with one load.
 static __global__ void __launch_bounds__(kUnevenChunk) uneven_scatter(UnevenArgs* __restrict__ a) {
   __shared__ int wc[kUnevenChunk / 32][kUnevenBins];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -135,7 +136,8 @@ static __global__ void __launch_bounds__(kUnevenChunk) uneven_scatter(UnevenArgs
   }
   __syncthreads();
   if (b >= 0 && b != kUnevenInvalid)
-    a->list[a->bucket_start[b] + a->chunk_base[blockIdx.x * kUnevenBins + b] + wc[warp][b] + rank] = (int)i;
+    a->list[a->bucket_start[b] + a->chunk_base[blockIdx.x * kUnevenBins + b] + wc[warp][b] + rank] =
+        __ldg(a->offsets + i);
 }
 
 // Persistent per-size kernel: CTAs stride over the tiles of bucket `bin`.
@@ -147,19 +149,27 @@ fft_uneven_kernel(const UnevenArgs* __restrict__ a, int bin, const typename E::T
   extern __shared__ __align__(16) unsigned char smem_raw[];
   long long* base = reinterpret_cast<long long*>(smem_raw + F::SMEM);
   const long long count = a->bucket_count[bin];
-  const int* list = a->list + a->bucket_start[bin];
-  const long long* offsets = a->offsets;
+  const long long* list = a->list + a->bucket_start[bin];
   const IndexedTile proto{a->in, a->out, base, 0, count};
-  for (long long tile0 = (long long)blockIdx.x * TPB; tile0 < count; tile0 += (long long)gridDim.x * TPB) {
+  const long long stride = (long long)gridDim.x * TPB;
+  // offset of this thread's transform in the current tile; the next tile's is
+  // loaded one iteration ahead, with its L2 prefetch
+  long long cur = 0;
+  if (threadIdx.x < TPB) {
+    const long long k = (long long)blockIdx.x * TPB + threadIdx.x;
+    cur = k < count ? __ldg(list + k) : 0;
+  }
+  for (long long tile0 = (long long)blockIdx.x * TPB; tile0 < count; tile0 += stride) {
     __syncthreads();  // the previous tile's readers of `base` and the staging buffer are done
     if (threadIdx.x < TPB) {
-      const long long k = tile0 + threadIdx.x;
-      base[threadIdx.x] = k < count ? __ldg(offsets + __ldg(list + k)) : 0;
+      base[threadIdx.x] = cur;
       // this CTA's next tile, transform by transform, into L2
-      const long long kn = k + (long long)gridDim.x * TPB;
+      const long long kn = tile0 + threadIdx.x + stride;
+      cur = 0;
       if (kn < count) {
-        const double2* q = a->in + __ldg(offsets + __ldg(list + kn));
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(q), "r"((unsigned)(PL::N * 16)) : "memory");
+        cur = __ldg(list + kn);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a->in + cur), "r"((unsigned)(PL::N * 16))
+                     : "memory");
       }
     }
     __syncthreads();

@@ -209,7 +209,7 @@ fftoc_status fftoc_autotune(int n, int engine, int64_t batch, fftoc_stream strea
  * beyond the buffers are the caller's responsibility, as for `batch` in the
  * per-size entry points.
  *
- * A plan owns the bucketing scratch (4 bytes per transform plus 64 bytes per
+ * A plan owns the bucketing scratch (8 bytes per transform plus 64 bytes per
  * 1024) and one CUDA graph: three bucketing kernels that group the transform
  * indices by size (stable), then one persistent kernel per size on parallel
  * graph branches, each using the plan currently chosen for its size
