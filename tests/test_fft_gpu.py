@@ -89,6 +89,37 @@ def test_every_compiled_plan(cuda, fftoc_lib, n, engine):
         F.plan_select(n, eid, cur["variant"])
 
 
+@pytest.mark.parametrize("n", SIZES)
+@pytest.mark.parametrize("engine", ["f64", "fx"])
+def test_code_forms_compute_the_same_bits(cuda, fftoc_lib, n, engine):
+    """Variants that share points per thread and radices differ only in how
+    the kernel is laid out (transforms per CTA, resident CTAs, L2 prefetch,
+    persistence, code forms): they must give the same bits, including for
+    transforms that take the rare input and output paths."""
+    import fft_onchip_gb300 as F
+    eid = F.ENGINES[engine]
+    cur = F.plan_query(n, eid)
+    x = inputs.normal(n, max(8, 4096 // n), seed=n + 11)
+    x[1] = 1e300 * x[1]                                      # outputs overflow: slow output path
+    x[2] = x[2] * 2.0 ** -1060                               # subnormal inputs: slow input path
+    x[3, ::2] *= 2.0 ** 40                                   # spread beyond 2^31 within a transform
+    x[4, n // 2] = np.inf                                    # non-finite: all-NaN transform
+    groups = {}
+    for v in range(cur["variants"]):
+        p = F.plan_query(n, eid, variant=v)
+        groups.setdefault((p["points_per_thread"], tuple(p["radix"])), []).append(v)
+    try:
+        for key, vs in groups.items():
+            outs = []
+            for v in vs:
+                F.plan_select(n, eid, v)
+                outs.append(run(cuda, x, engine))
+            for v, o in zip(vs[1:], outs[1:]):
+                assert np.array_equal(o.view(np.int64), outs[0].view(np.int64)), (n, engine, key, vs[0], v)
+    finally:
+        F.plan_select(n, eid, cur["variant"])
+
+
 def test_autotune_selects_a_valid_plan(cuda, fftoc_lib):
     import fft_onchip_gb300 as F
     cur = F.plan_query(256, F.ENGINE_FX)
