@@ -321,44 +321,53 @@ FFTOC_HD void dft8(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
   }
 }
 
-// 16-point DFT: two 8-point DFTs (even / odd samples) and a radix-2 combine
-// with W16^k.
+// 16-point DFT as 4 x 4: with n = 4*n1 + n2 and k = k1 + 4*k2,
+//   X[k1 + 4 k2] = sum_n2 W4^(n2 k2) * (W16^(n2 k1) * sum_n1 x[4 n1 + n2] W4^(n1 k1)):
+// four DFT4s over n1, the nine non-trivial W16^(n2 k1), four DFT4s over n2,
+// and a transposition of the outputs (register renaming).
 template <class E, int B, int ST, int PP>
 FFTOC_HD void dft16(typename E::S (&re)[PP], typename E::S (&im)[PP]) {
   using S = typename E::S;
   using K = Konst<E>;
-  // even samples at B + 2m*ST, odd at B + (2m+1)*ST
-  dft8<E, B, 2 * ST, PP>(re, im);
-  dft8<E, B + ST, 2 * ST, PP>(re, im);
-  // O[k] *= W16^k, k = 1..7
-  {
-    S r, i;
-    // k=1: (c8, -s8)
-    r = re[B + 3 * ST]; i = im[B + 3 * ST]; E::cmulk(r, i, K::c8(), K::ns8()); re[B + 3 * ST] = r; im[B + 3 * ST] = i;
-    // k=2: (1-i)/sqrt2
-    r = re[B + 5 * ST]; i = im[B + 5 * ST];
-    re[B + 5 * ST] = E::mulc(E::add(r, i), K::h()); im[B + 5 * ST] = E::mulc(E::sub(i, r), K::h());
-    // k=3: (s8, -c8)
-    r = re[B + 7 * ST]; i = im[B + 7 * ST]; E::cmulk(r, i, K::s8(), K::nc8()); re[B + 7 * ST] = r; im[B + 7 * ST] = i;
-    // k=4: -i
-    r = re[B + 9 * ST]; i = im[B + 9 * ST]; re[B + 9 * ST] = i; im[B + 9 * ST] = E::sub(S(0), r);
-    // k=5: (-s8, -c8)
-    r = re[B + 11 * ST]; i = im[B + 11 * ST]; E::cmulk(r, i, K::ns8(), K::nc8()); re[B + 11 * ST] = r; im[B + 11 * ST] = i;
-    // k=6: (-1-i)/sqrt2
-    r = re[B + 13 * ST]; i = im[B + 13 * ST];
-    re[B + 13 * ST] = E::mulc(E::sub(i, r), K::h()); im[B + 13 * ST] = E::mulc(E::add(r, i), K::nh());
-    // k=7: (-c8, -s8)
-    r = re[B + 15 * ST]; i = im[B + 15 * ST]; E::cmulk(r, i, K::nc8(), K::ns8()); re[B + 15 * ST] = r; im[B + 15 * ST] = i;
-  }
-  // combine: X[k] = E[k] + O[k], X[k+8] = E[k] - O[k]; E[k] at B + 2k*ST, O[k] at B + (2k+1)*ST
+  // y[n2][k1] at B + (n2 + 4 k1) ST
+  dft4<E, B, 4 * ST, PP>(re, im);
+  dft4<E, B + ST, 4 * ST, PP>(re, im);
+  dft4<E, B + 2 * ST, 4 * ST, PP>(re, im);
+  dft4<E, B + 3 * ST, 4 * ST, PP>(re, im);
+  auto at = [](int n2, int k1) { return B + (n2 + 4 * k1) * ST; };
+  S r, i;
+  // W16^1 = (c8, -s8)
+  r = re[at(1, 1)]; i = im[at(1, 1)]; E::cmulk(r, i, K::c8(), K::ns8()); re[at(1, 1)] = r; im[at(1, 1)] = i;
+  // W16^2 = (1 - i)/sqrt2, at (1, 2) and (2, 1)
+  r = re[at(1, 2)]; i = im[at(1, 2)];
+  re[at(1, 2)] = E::mulc(E::add(r, i), K::h()); im[at(1, 2)] = E::mulc(E::sub(i, r), K::h());
+  r = re[at(2, 1)]; i = im[at(2, 1)];
+  re[at(2, 1)] = E::mulc(E::add(r, i), K::h()); im[at(2, 1)] = E::mulc(E::sub(i, r), K::h());
+  // W16^3 = (s8, -c8), at (1, 3) and (3, 1)
+  r = re[at(1, 3)]; i = im[at(1, 3)]; E::cmulk(r, i, K::s8(), K::nc8()); re[at(1, 3)] = r; im[at(1, 3)] = i;
+  r = re[at(3, 1)]; i = im[at(3, 1)]; E::cmulk(r, i, K::s8(), K::nc8()); re[at(3, 1)] = r; im[at(3, 1)] = i;
+  // W16^4 = -i, at (2, 2)
+  r = re[at(2, 2)]; i = im[at(2, 2)]; re[at(2, 2)] = i; im[at(2, 2)] = E::sub(S(0), r);
+  // W16^6 = (-1 - i)/sqrt2, at (2, 3) and (3, 2)
+  r = re[at(2, 3)]; i = im[at(2, 3)];
+  re[at(2, 3)] = E::mulc(E::sub(i, r), K::h()); im[at(2, 3)] = E::mulc(E::add(r, i), K::nh());
+  r = re[at(3, 2)]; i = im[at(3, 2)];
+  re[at(3, 2)] = E::mulc(E::sub(i, r), K::h()); im[at(3, 2)] = E::mulc(E::add(r, i), K::nh());
+  // W16^9 = (-c8, s8), at (3, 3)
+  r = re[at(3, 3)]; i = im[at(3, 3)]; E::cmulk(r, i, K::nc8(), K::s8()); re[at(3, 3)] = r; im[at(3, 3)] = i;
+  // DFT4 over n2 for each k1: inputs at B + (4 k1 + n2) ST, outputs X[k1 + 4 k2] at B + (4 k1 + k2) ST
+  dft4<E, B, ST, PP>(re, im);
+  dft4<E, B + 4 * ST, ST, PP>(re, im);
+  dft4<E, B + 8 * ST, ST, PP>(re, im);
+  dft4<E, B + 12 * ST, ST, PP>(re, im);
   S xr[16], xi[16];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const S er = re[B + 2 * k * ST], ei = im[B + 2 * k * ST];
-    const S orr = re[B + (2 * k + 1) * ST], oi = im[B + (2 * k + 1) * ST];
-    xr[k] = E::add(er, orr); xi[k] = E::add(ei, oi);
-    xr[k + 8] = E::sub(er, orr); xi[k + 8] = E::sub(ei, oi);
-  }
+  for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) {
+      xr[k1 + 4 * k2] = re[B + (4 * k1 + k2) * ST];
+      xi[k1 + 4 * k2] = im[B + (4 * k1 + k2) * ST];
+    }
 #pragma unroll
   for (int k = 0; k < 16; ++k) { re[B + k * ST] = xr[k]; im[B + k * ST] = xi[k]; }
 }
