@@ -43,6 +43,7 @@ struct PlanT {
   static constexpr bool OUTLINE_SLOW_IN = false;  // batched kernel: rare input path out of line (OutlinedSlowIn<>)
   static constexpr bool IMAD_SPLIT = false;  // fixed point: low limbs by integer multiply-add (ImadSplit<>)
   static constexpr bool OUT_HI_ZERO = false;  // fixed point: zero test on the converted word (OutHiZero<>)
+  static constexpr bool NO_STAGE = false;  // fewer than 8 threads per transform: direct HBM access (NoStage<>)
   static constexpr int R[4] = {R0, R1, R2, R3};
   static constexpr int S = (R0 > 1) + (R1 > 1) + (R2 > 1) + (R3 > 1);
   static constexpr int T = N / P;
@@ -237,6 +238,16 @@ struct ImadSplit : PL {
 template <class PL>
 struct OutHiZero : PL {
   static constexpr bool OUT_HI_ZERO = true;
+};
+
+// A plan with fewer than 8 threads per transform that loads and stores HBM
+// directly instead of staging its tile through shared memory.  With T
+// threads per transform each warp access still covers whole 32-byte sectors
+// for T >= 2; it pays off where the staging round trip costs more than the
+// spread of the access (measured: T = 4).
+template <class PL>
+struct NoStage : PL {
+  static constexpr bool NO_STAGE = true;
 };
 
 // The engine a plan's kernels compute with: the fixed-point engine in the

@@ -171,7 +171,7 @@ struct Fft {
   static constexpr int SH = PL::R[0] >= 16 ? 4 : 3;
   static constexpr int NP = N + (N >> SH);
   static constexpr int THREADS = T * TPB;
-  static constexpr bool STAGED = T < 8;  // small N: stage HBM tiles through smem
+  static constexpr bool STAGED = T < 8 && !PL::NO_STAGE;  // small N: stage HBM tiles through smem
   static constexpr int SMEM = TPB * NP * 16 + 64;
 
   // 16-byte slot of element e of block-local transform j

@@ -21,7 +21,7 @@ SIZES = _lib.SIZES
 
 def code_str(p):
     """The code-form flags of a plan, e.g. 'outlined-in,imad-split'."""
-    names = ((1, "outlined-in"), (2, "imad-split"), (4, "out-hi-zero"))
+    names = ((1, "outlined-in"), (2, "imad-split"), (4, "out-hi-zero"), (8, "direct-io"))
     return ",".join(nm for bit, nm in names if p.get("code_flags", 0) & bit)
 
 

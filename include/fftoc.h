@@ -169,12 +169,14 @@ typedef struct {
   int stages;                 /* shared-memory stages (persistent plans)     */
   int prefetch;               /* 1: each CTA prefetches, into L2, the tile of
                                  the CTA one full wave later                 */
-  int code_flags;             /* code forms of the fixed-point kernels (same
-                                 results): FFTOC_CODE_* bits                 */
+  int code_flags;             /* code and memory-access forms of the plan's
+                                 kernels (same results): FFTOC_CODE_* bits   */
 } fftoc_plan_info;
 #define FFTOC_CODE_OUTLINED_SLOW_INPUT 1 /* rare input conversions out of line */
 #define FFTOC_CODE_IMAD_SPLIT 2          /* limb splits by integer multiply-add */
 #define FFTOC_CODE_OUT_HI_ZERO 4         /* output zero test on the high word */
+#define FFTOC_CODE_DIRECT_IO 8           /* small n: HBM accessed directly, no
+                                            shared-memory staging of the tile */
 
 /* Plan currently used for (n, engine). */
 fftoc_status fftoc_plan_query(int n, int engine, fftoc_plan_info *info);
