@@ -513,7 +513,7 @@ def bench_onchip(args, torch, F):
     from fft_onchip_gb300 import onchip
     out = {"workload": "on-chip repeat mode: (32 x SMs) transforms per pass resident in shared memory, "
                        "(t(1100) - t(100)) / 1000 per pass, no HBM traffic in the difference", "per_n": {}}
-    for n in (8, 64, 128, 256, 512, 4096):
+    for n in (8, 16, 64, 128, 256, 512, 4096):
         r = onchip.time_onchip(n, F.ENGINE_AUTO)
         out["per_n"][str(n)] = {k: r[k] for k in ("us_per_pass", "ffts_per_s", "transforms_per_block", "blocks")}
     return out
