@@ -1,7 +1,8 @@
 """ctypes front end of the CPU oracle (test infrastructure only).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
-module, as the checker.  The product library never imports it.
+module, to check results and time the CPU baseline.  The product library never
+imports it.
 
 Arrays are numpy complex128 of shape (batch, n) (interleaved re/im doubles,
 transforms back to back), matching the layout of the reference harness
