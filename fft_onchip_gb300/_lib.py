@@ -105,6 +105,7 @@ class PlanInfo(ctypes.Structure):
         ("stages", ctypes.c_int),
         ("prefetch", ctypes.c_int),
         ("code_flags", ctypes.c_int),
+        ("uneven_variant", ctypes.c_int),
     ]
 
 
@@ -224,6 +225,7 @@ def _info_dict(info):
         "stages": info.stages,
         "prefetch": info.prefetch,
         "code_flags": info.code_flags,
+        "uneven_variant": info.uneven_variant,
     }
 
 

@@ -345,7 +345,9 @@ fftoc_status plan_query(int n, int engine, int variant, fftoc_plan_info* info) {
   if (eng == FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_UNSUPPORTED, "DMMA engine not available for n=" + std::to_string(n));
   if (is_split_engine(eng)) {
     if (variant > 0) return fail(FFTOC_ERR_INVALID_VALUE, "no such plan variant");
-    return split_plan_info(n, split_kind_of(eng), info);
+    const fftoc_status st = split_plan_info(n, split_kind_of(eng), info);
+    if (st == FFTOC_OK) info->uneven_variant = -1;  // the uneven path has no split-form kernels
+    return st;
   }
   const int slot = eng == FFTOC_ENGINE_FX ? 1 : 0;
   const SizeVariants& sv = host_variants(slot)[idx];
@@ -367,6 +369,7 @@ fftoc_status plan_query(int n, int engine, int variant, fftoc_plan_info* info) {
   info->stages = d.stages;
   info->prefetch = d.prefetch;
   info->code_flags = d.code_flags;
+  info->uneven_variant = uneven_variant(slot, idx);
   return FFTOC_OK;
 }
 

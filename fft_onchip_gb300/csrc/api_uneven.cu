@@ -64,6 +64,25 @@ const SizeVariants* uneven_variants(int slot) {
   return table[slot];
 }
 
+}  // namespace
+
+// Plan of size index i for the uneven path: while the size's choice is the
+// library default (variant 0), its UnevenDefault<> plan if it has one; else
+// the chosen plan if it has an uneven kernel; else the first plan that has one.
+int uneven_variant(int slot, int i) {
+  const SizeVariants& sv = uneven_variants(slot)[i];
+  const int c = chosen_variant(slot, i);
+  if (c == 0)
+    for (int v = 0; v < sv.count; ++v)
+      if (sv.v[v].uneven_default && sv.v[v].fn_uneven) return v;
+  if (c < sv.count && sv.v[c].fn_uneven) return c;
+  for (int v = 0; v < sv.count; ++v)
+    if (sv.v[v].fn_uneven) return v;
+  return -1;
+}
+
+namespace {
+
 struct UnevenDevice {
   std::once_flag once;
   fftoc_status status = FFTOC_OK;
@@ -106,15 +125,7 @@ fftoc_status cuda_err(cudaError_t e, const char* what) {
                    std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// Plan of size index i for the uneven path: the chosen plan if it has an
-// uneven kernel, else the first plan that has one.
-int uneven_choice(const UnevenDevice& u, int slot, int i) {
-  const int c = chosen_variant(slot, i);
-  if (c < u.var[slot][i].count && u.var[slot][i].v[c].fn_uneven) return c;
-  for (int v = 0; v < u.var[slot][i].count; ++v)
-    if (u.var[slot][i].v[v].fn_uneven) return v;
-  return -1;
-}
+int uneven_choice(const UnevenDevice&, int slot, int i) { return uneven_variant(slot, i); }
 
 fftoc_status resolve_kernels(fftoc_uneven_plan p, const UnevenDevice& u, bool* changed) {
   *changed = false;

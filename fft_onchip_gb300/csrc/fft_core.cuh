@@ -44,6 +44,7 @@ struct PlanT {
   static constexpr bool IMAD_SPLIT = false;  // fixed point: low limbs by integer multiply-add (ImadSplit<>)
   static constexpr bool OUT_HI_ZERO = false;  // fixed point: zero test on the converted word (OutHiZero<>)
   static constexpr bool NO_STAGE = false;  // fewer than 8 threads per transform: direct HBM access (NoStage<>)
+  static constexpr bool UNEVEN_DEFAULT = false;  // the uneven path's default plan for its size (UnevenDefault<>)
   static constexpr int R[4] = {R0, R1, R2, R3};
   static constexpr int S = (R0 > 1) + (R1 > 1) + (R2 > 1) + (R3 > 1);
   static constexpr int T = N / P;
@@ -248,6 +249,14 @@ struct OutHiZero : PL {
 template <class PL>
 struct NoStage : PL {
   static constexpr bool NO_STAGE = true;
+};
+
+// The plan the uneven-batch path uses for its size while the size's plan
+// choice is the library default (its persistent kernels measured faster
+// with it than with the batched default).
+template <class PL>
+struct UnevenDefault : PL {
+  static constexpr bool UNEVEN_DEFAULT = true;
 };
 
 // The engine a plan's kernels compute with: the fixed-point engine in the

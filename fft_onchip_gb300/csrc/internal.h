@@ -34,6 +34,7 @@ struct KernelDesc {
   int blocks_per_sm = 0;     // resident CTAs per SM (filled at device set-up)
   int prefetch = 0;          // 1: L2 prefetch one wave ahead (Prefetched<> plans)
   int code_flags = 0;        // FFTOC_CODE_* bits of the plan
+  int uneven_default = 0;    // 1: the uneven path's default plan for this size (UnevenDefault<>)
   // uneven-batch kernel of the same plan (nullptr for TMA-prefetching plans)
   const void* fn_uneven = nullptr;
   int smem_uneven = 0;
@@ -137,5 +138,7 @@ int resolved_engine(int n, int engine);
 // error flag and SM count (device set-up on first use).
 fftoc_status device_plan_resources(int slot, int idx, int var, const void** tw, int** err, int* sms);
 fftoc_status set_error(fftoc_status st, const std::string& msg);
+// Plan variant the uneven-batch path uses for (engine slot, size index), or -1.
+int uneven_variant(int slot, int idx);
 
 }  // namespace fftoc

@@ -171,6 +171,10 @@ typedef struct {
                                  the CTA one full wave later                 */
   int code_flags;             /* code and memory-access forms of the plan's
                                  kernels (same results): FFTOC_CODE_* bits   */
+  int uneven_variant;         /* plan variant the uneven-batch path and the
+                                 serving loop use for this size (equal to the
+                                 chosen variant unless the choice is the
+                                 default variant 0)                          */
 } fftoc_plan_info;
 #define FFTOC_CODE_OUTLINED_SLOW_INPUT 1 /* rare input conversions out of line */
 #define FFTOC_CODE_IMAD_SPLIT 2          /* limb splits by integer multiply-add */
@@ -213,10 +217,12 @@ fftoc_status fftoc_autotune(int n, int engine, int64_t batch, fftoc_stream strea
  *
  * A plan owns the bucketing scratch (8 bytes per transform plus 64 bytes per
  * 1024) and one CUDA graph: three bucketing kernels that group the transform
- * indices by size (stable), then one persistent kernel per size on parallel
+ * offsets by size (stable), then one persistent kernel per size on parallel
  * graph branches, each using the plan currently chosen for its size
- * (fftoc_plan_select / fftoc_autotune; TMA-prefetching plans fall back to
- * the size's first plan without prefetch).  fftoc_uneven_execute enqueues a
+ * (fftoc_plan_select / fftoc_autotune; while a size's choice is the default
+ * variant 0 the path uses its own default plan for that size, and
+ * TMA-prefetching plans fall back to the size's first plan without prefetch;
+ * fftoc_plan_info.uneven_variant names the plan used).  fftoc_uneven_execute enqueues a
  * 1-thread argument kernel and the graph on `stream` and is asynchronous; it
  * re-captures the graph when a size's plan choice changed.  One plan runs one
  * batch at a time: executions of one plan must be ordered (same stream, or

@@ -53,7 +53,14 @@ def test_alone_equals_in_mix_and_matches_oracle(cuda, fftoc_lib):
     assert st["batches"] < 40  # requests were batched together
     y_mix = reqs[32].out.numpy()
     assert np.array_equal(bits(y_mix), bits(y_alone))
-    ref = F.fft(cuda.from_numpy(target).cuda()).cpu().numpy()
+    # the batched entry point on the plan the serving loop's uneven graphs use
+    eng = F.auto_engine(256)
+    q = F.plan_query(256, eng)
+    try:
+        F.plan_select(256, eng, q["uneven_variant"])
+        ref = F.fft(cuda.from_numpy(target).cuda()).cpu().numpy()
+    finally:
+        F.plan_select(256, eng, q["variant"])
     assert np.array_equal(bits(y_mix), bits(ref))
     for x, r in zip(xs, reqs):
         assert O.rel_l2(r.out.numpy(), O.fft_f64(x)) < TOL

@@ -3,6 +3,8 @@ one CUDA graph): parity with the oracle, bit-identity with the per-size
 batched entry points on the same plans, the per-size comparison path, and
 the edge cases (empty, gaps, shuffled order, in place, bad entries, plan
 changes, plan growth)."""
+from contextlib import contextmanager
+
 import numpy as np
 import pytest
 
@@ -19,16 +21,36 @@ def dev(torch, a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
+@contextmanager
+def uneven_plans(F, engine="auto"):
+    """Select, for every size, the plan the uneven path uses (plan_query's
+    uneven_variant), so that the batched entry point runs the same
+    arithmetic; restore the choices afterwards."""
+    saved = []
+    for n in SIZES:
+        e = F.ENGINES[engine] or F.auto_engine(n)
+        q = F.plan_query(n, e)
+        saved.append((n, e, q["variant"]))
+        F.plan_select(n, e, q["uneven_variant"])
+    try:
+        yield
+    finally:
+        for n, e, v in saved:
+            F.plan_select(n, e, v)
+
+
 def batched_reference(torch, F, xf, off, ns, engine="auto"):
     """Each size's transforms gathered into a contiguous batch, run through
-    the per-size entry point, scattered back (host side)."""
+    the per-size entry point on the uneven path's plans, scattered back (host
+    side)."""
     out = np.zeros_like(xf)
-    for n in np.unique(ns):
-        idx = np.nonzero(ns == n)[0]
-        rows = np.stack([xf[off[i]:off[i] + n] for i in idx])
-        y = F.fft(dev(torch, rows), engine=engine).cpu().numpy()
-        for k, i in enumerate(idx):
-            out[off[i]:off[i] + n] = y[k]
+    with uneven_plans(F, engine):
+        for n in np.unique(ns):
+            idx = np.nonzero(ns == n)[0]
+            rows = np.stack([xf[off[i]:off[i] + n] for i in idx])
+            y = F.fft(dev(torch, rows), engine=engine).cpu().numpy()
+            for k, i in enumerate(idx):
+                out[off[i]:off[i] + n] = y[k]
     return out
 
 
@@ -109,7 +131,8 @@ def test_single_size_and_single_transform(cuda, fftoc_lib):
             off, total = inputs.uneven_layout(ns)
             xf = inputs.uniform_flat(total, seed=n + count)
             y = F.fft_uneven(dev(cuda, xf), dev(cuda, off), dev(cuda, ns)).cpu().numpy()
-            ref = F.fft(dev(cuda, xf.reshape(count, n))).cpu().numpy().reshape(-1)
+            with uneven_plans(F):
+                ref = F.fft(dev(cuda, xf.reshape(count, n))).cpu().numpy().reshape(-1)
             assert np.array_equal(y.view(np.uint64), ref.view(np.uint64)), (n, count)
 
 
@@ -206,9 +229,10 @@ def test_full_size_mixed_batch_matches_per_size_path(cuda, fftoc_lib):
     sample = np.arange(0, 200000, 997)
     assert oracle_err(xf, yh, off[sample], ns[sample]) < TOL
     # per-size batched launches on device copies of each size's transforms
-    for n in SIZES:
-        idx = np.nonzero(ns == n)[0]
-        gather = (cuda.from_numpy(off[idx]).cuda()[:, None] + cuda.arange(n, device="cuda")[None, :]).reshape(-1)
-        rows = d_x[gather].reshape(len(idx), n)
-        ref = F.fft(rows)
-        assert cuda.equal(bits(y[gather].reshape(len(idx), n)), bits(ref)), n
+    with uneven_plans(F):
+        for n in SIZES:
+            idx = np.nonzero(ns == n)[0]
+            gather = (cuda.from_numpy(off[idx]).cuda()[:, None] + cuda.arange(n, device="cuda")[None, :]).reshape(-1)
+            rows = d_x[gather].reshape(len(idx), n)
+            ref = F.fft(rows)
+            assert cuda.equal(bits(y[gather].reshape(len(idx), n)), bits(ref)), n
