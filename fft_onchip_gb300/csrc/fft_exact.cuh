@@ -64,7 +64,9 @@ struct ExactPlan {
   static constexpr int RED_OFF = DATA_OFF + DATA_BYTES;
   static constexpr int BAR_OFF = RED_OFF + ((TPB * 4 + 15) / 16) * 16;
   static constexpr int SMEM = BAR_OFF + 8 * G + 8;
-  static constexpr int TMEM_COLS = 512;                             // 6 orders x 32 x G <= 384
+  // 6 orders x 32 columns per group, rounded up to a power of two: one group
+  // takes 256 columns, so two one-group CTAs share an SM's TMEM
+  static constexpr int TMEM_COLS = G == 1 ? 256 : 512;
   static_assert(32 * kExactOrders * G <= TMEM_COLS, "accumulators fit in TMEM");
   static_assert(G <= 2, "named barriers 1 and 2 serve the two groups");
   static constexpr bool GROUP_LOCAL = T <= 128;

@@ -1,8 +1,9 @@
 // fftoc — split-precision form instantiations: one plan per size (radix-16
 // GEMM passes, a radix 2/4/8 last pass where N is not a power of 16), for
-// the BF16x3 and TF32x2 operand splits (two CTAs per SM) and the exact-slice
-// form (fft_exact.cuh, one CTA per SM: its accumulators fill TMEM).  256
-// threads = two groups of 128 butterfly rows per CTA.
+// the BF16x3 and TF32x2 operand splits (two CTAs per SM, 256 threads = two
+// groups of 128 butterfly rows per CTA) and the exact-slice form
+// (fft_exact.cuh: one group per CTA and two CTAs per SM up to N = 2048, whose
+// accumulators then share TMEM; two groups and one CTA per SM at N = 4096).
 #include "fft_exact.cuh"
 #include "fft_split.cuh"
 #include "internal.h"
@@ -39,10 +40,10 @@ void describe(SplitDesc* d) {
   add_split<KIND, PlanT<4096, 16, 1, 16, 16, 16, 1, 2>>(d[9]);
 }
 
-template <class PL>
+template <class PL, int G>
 void add_exact(SplitDesc& d) {
-  using XP = ExactPlan<PL, 2>;
-  d.fn = (const void*)&fft_exact_kernel<PL, 2>;
+  using XP = ExactPlan<PL, G>;
+  d.fn = (const void*)&fft_exact_kernel<PL, G>;
   d.threads = XP::THREADS;
   d.tpb = PL::TPB;
   d.smem = XP::SMEM;
@@ -55,15 +56,17 @@ void add_exact(SplitDesc& d) {
 }
 
 void describe_exact(SplitDesc* d) {
-  add_exact<PlanT<16, 16, 256, 16>>(d[1]);
-  add_exact<PlanT<32, 16, 128, 16, 2>>(d[2]);
-  add_exact<PlanT<64, 16, 64, 16, 4>>(d[3]);
-  add_exact<PlanT<128, 16, 32, 16, 8>>(d[4]);
-  add_exact<PlanT<256, 16, 16, 16, 16>>(d[5]);
-  add_exact<PlanT<512, 16, 8, 16, 16, 2>>(d[6]);
-  add_exact<PlanT<1024, 16, 4, 16, 16, 4>>(d[7]);
-  add_exact<PlanT<2048, 16, 2, 16, 16, 8>>(d[8]);
-  add_exact<PlanT<4096, 16, 1, 16, 16, 16>>(d[9]);
+  // one 128-thread group per CTA (two CTAs per SM) where a transform fits in
+  // 128 threads: measured 1.1-1.33x the two-group CTA; N=4096 needs both groups
+  add_exact<PlanT<16, 16, 128, 16>, 1>(d[1]);
+  add_exact<PlanT<32, 16, 64, 16, 2>, 1>(d[2]);
+  add_exact<PlanT<64, 16, 32, 16, 4>, 1>(d[3]);
+  add_exact<PlanT<128, 16, 16, 16, 8>, 1>(d[4]);
+  add_exact<PlanT<256, 16, 8, 16, 16>, 1>(d[5]);
+  add_exact<PlanT<512, 16, 4, 16, 16, 2>, 1>(d[6]);
+  add_exact<PlanT<1024, 16, 2, 16, 16, 4>, 1>(d[7]);
+  add_exact<PlanT<2048, 16, 1, 16, 16, 8>, 1>(d[8]);
+  add_exact<PlanT<4096, 16, 1, 16, 16, 16>, 2>(d[9]);
 }
 
 }  // namespace
