@@ -69,10 +69,14 @@ def main():
     ap.add_argument("--sizes", default="8,64,128,256,512,4096")
     ap.add_argument("--engine", default="auto")
     ap.add_argument("--sm-multiplier", type=int, default=32)
+    ap.add_argument("--saturation", default="",
+                    help="comma list of blocks-per-SM multipliers to sweep (the reference's saturation test)")
     a = ap.parse_args()
     eng = _lib.ENGINES[a.engine]
+    mults = [int(v) for v in a.saturation.split(",") if v] or [a.sm_multiplier]
     for n in [int(v) for v in a.sizes.split(",")]:
-        print(json.dumps(time_onchip(n, eng, a.sm_multiplier)), flush=True)
+        for m in mults:
+            print(json.dumps(time_onchip(n, eng, m)), flush=True)
 
 
 if __name__ == "__main__":

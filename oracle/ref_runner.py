@@ -103,32 +103,51 @@ def fixtures():
         print(name, batch)
 
 
-def timing(sm_multiplier=32):
-    """On-chip us per pass: (t(1100) - t(100)) / 1000, grid = 32*SMs/(UPB*FPU)
-    (includes/testing.cuh:68-69,115-124), data replicated per block."""
+def _time_executor(drv, name, sm_multiplier):
+    """us per on-chip pass of one executor: (t(1100) - t(100)) / 1000 with
+    grid = sm_multiplier*SMs/(UPB*FPU) (includes/testing.cuh:68-69,115-124)."""
     import torch
-    drv = Driver()
+    n, threads, staged = EXECUTORS[name]
     sms = torch.cuda.get_device_properties(0).multi_processor_count
+    per_block = staged // n
+    blocks = max(1, (sm_multiplier * sms) // per_block)
+    d = torch.randn(blocks * per_block, n, dtype=torch.complex128, device="cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    drv.launch(name, d.data_ptr(), blocks, 10)
+    torch.cuda.synchronize()
+    ev[0].record()
+    drv.launch(name, d.data_ptr(), blocks, 100)
+    ev[1].record()
+    drv.launch(name, d.data_ptr(), blocks, 1100)
+    ev[2].record()
+    torch.cuda.synchronize()
+    us = (ev[1].elapsed_time(ev[2]) - ev[0].elapsed_time(ev[1])) * 1e3 / 1000.0
+    ffts = blocks * per_block
+    return {"n": n, "sm_multiplier": sm_multiplier, "us_per_pass": us, "ffts_per_pass": ffts,
+            "ffts_per_s": ffts / (us * 1e-6)}
+
+
+def timing(sm_multiplier=32):
+    """On-chip us per pass of every executor at the harness's default grid
+    (data replicated per block)."""
+    drv = Driver()
     out = {}
-    for name, (n, threads, staged) in EXECUTORS.items():
-        per_block = staged // n
-        blocks = (sm_multiplier * sms) // per_block
-        d = torch.randn(blocks * per_block, n, dtype=torch.complex128, device="cuda")
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-        drv.launch(name, d.data_ptr(), blocks, 10)
-        torch.cuda.synchronize()
-        ev[0].record()
-        drv.launch(name, d.data_ptr(), blocks, 100)
-        ev[1].record()
-        drv.launch(name, d.data_ptr(), blocks, 1100)
-        ev[2].record()
-        torch.cuda.synchronize()
-        t100 = ev[0].elapsed_time(ev[1]) * 1e3
-        t1100 = ev[1].elapsed_time(ev[2]) * 1e3
-        us = (t1100 - t100) / 1000.0
-        ffts = blocks * per_block
-        out[name] = {"n": n, "us_per_pass": us, "ffts_per_pass": ffts, "ffts_per_s": ffts / (us * 1e-6)}
+    for name in EXECUTORS:
+        out[name] = _time_executor(drv, name, sm_multiplier)
         print(json.dumps({name: out[name]}))
+    return out
+
+
+def saturation(multipliers=(4, 8, 16, 32, 64, 128, 256)):
+    """The reference's saturation sweep (src/saturation.cu:36-44): per-pass
+    time of its tensor executors against blocks per SM."""
+    drv = Driver()
+    out = {}
+    for name in ("ref_tensor_fft_8", "ref_tensor_fft_64", "ref_tensor_fft_128", "ref_tensor_fft_256",
+                 "ref_tensor_fft_512"):
+        out[name] = [_time_executor(drv, name, m) for m in multipliers]
+        for r in out[name]:
+            print(json.dumps({name: r}), flush=True)
     return out
 
 
@@ -167,5 +186,7 @@ if __name__ == "__main__":
         fixtures()
     elif what == "stream":
         stream()
+    elif what == "saturation":
+        saturation()
     else:
         timing()
