@@ -111,3 +111,31 @@ def test_missing_library_fails_loudly(tmp_path):
             _lib.load(str(tmp_path / "libfftoc.so"))
         finally:
             _lib._lib = saved
+
+
+@pytest.mark.parametrize("n", _lib.SIZES)
+@pytest.mark.parametrize("engine", ["f64", "fx"])
+def test_plan_code_flags_and_uneven_variant(fftoc_lib, n, engine):
+    """code_flags carries only the documented bits; the uneven path uses its
+    own default plan while the size's choice is variant 0, else the chosen
+    plan (never a persistent one)."""
+    from fft_onchip_gb300 import tune
+    eid = _lib.ENGINES[engine]
+    cur = _lib.plan_query(n, eid)
+    nv = cur["variants"]
+    for v in range(nv):
+        p = _lib.plan_query(n, eid, variant=v)
+        assert p["code_flags"] & ~15 == 0
+        assert bool(p["code_flags"]) == bool(tune.code_str(p))
+    uv = cur["uneven_variant"]
+    assert 0 <= uv < nv and not _lib.plan_query(n, eid, variant=uv)["persistent"]
+    try:
+        for v in range(1, nv):
+            _lib.plan_select(n, eid, v)
+            got = _lib.plan_query(n, eid)["uneven_variant"]
+            if _lib.plan_query(n, eid, variant=v)["persistent"]:
+                assert got != v and not _lib.plan_query(n, eid, variant=got)["persistent"]
+            else:
+                assert got == v
+    finally:
+        _lib.plan_select(n, eid, cur["variant"])
