@@ -2,7 +2,7 @@
  * fftoc oracle — CPU restatement of gprabowski/fft_onchip's batched forward
  * complex FFT path.  TEST INFRASTRUCTURE ONLY: the product library never links,
  * loads or calls anything in this file; tests, smoke() and the CPU-baseline leg
- * of bench.py use it as the checker.
+ * of bench.py use it to check and time results.
  *
  * Convention (reference includes/reference.cuh:10-12 — cuFFTDx C2C, forward,
  * double, no scaling; and every executor's pow_theta, e.g.
