@@ -64,16 +64,28 @@ def saturation(n, multipliers=range(4, 257, 4), engine=_lib.ENGINE_AUTO):
     return [time_onchip(n, engine, m) for m in multipliers]
 
 
+def apply_plans(spec, engine=_lib.ENGINE_AUTO):
+    """Select plan variants from 'N:variant,...' (the engine's choice per N
+    when engine is AUTO), as bench.py's --plan does."""
+    for item in filter(None, spec.split(",")):
+        pn, pv = item.split(":")
+        n = int(pn)
+        eng = engine if engine != _lib.ENGINE_AUTO else load().fftoc_auto_engine(n)
+        _lib.plan_select(n, eng, int(pv))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--sizes", default="8,64,128,256,512,4096")
     ap.add_argument("--engine", default="auto")
     ap.add_argument("--sm-multiplier", type=int, default=32)
+    ap.add_argument("--plan", default="", help="N:variant,... plan overrides (default: the library's choice)")
     ap.add_argument("--saturation", default="",
                     help="comma list of blocks-per-SM multipliers to sweep (the reference's saturation test)")
     a = ap.parse_args()
     eng = _lib.ENGINES[a.engine]
     mults = [int(v) for v in a.saturation.split(",") if v] or [a.sm_multiplier]
+    apply_plans(a.plan, eng)
     for n in [int(v) for v in a.sizes.split(",")]:
         for m in mults:
             print(json.dumps(time_onchip(n, eng, m)), flush=True)

@@ -139,3 +139,34 @@ def test_plan_code_flags_and_uneven_variant(fftoc_lib, n, engine):
                 assert got == v
     finally:
         _lib.plan_select(n, eid, cur["variant"])
+
+
+@pytest.mark.parametrize("n", [128, 256, 512])
+def test_small_cta_defaults_per_engine(fftoc_lib, n):
+    """At N = 128, 256 and 512 the fixed-point default is the IEEE engine's
+    default plan in 64-thread CTAs; the larger-CTA plan follows it and stays
+    the plan of the uneven-batch kernels."""
+    fx0, fx1 = (_lib.plan_query(n, _lib.ENGINE_FX, variant=v) for v in (0, 1))
+    f0, f1 = (_lib.plan_query(n, _lib.ENGINE_F64, variant=v) for v in (0, 1))
+    for a, b in ((fx0, f1), (fx1, f0)):
+        assert (a["radix"], a["points_per_thread"], a["transforms_per_block"]) == \
+               (b["radix"], b["points_per_thread"], b["transforms_per_block"])
+    assert (fx0["radix"], fx0["points_per_thread"]) == (fx1["radix"], fx1["points_per_thread"])
+    assert fx0["threads_per_transform"] * fx0["transforms_per_block"] == 64
+    assert fx0["transforms_per_block"] < fx1["transforms_per_block"]
+    assert _lib.plan_query(n, _lib.ENGINE_FX, variant=0)["uneven_variant"] == 1
+
+
+def test_onchip_plan_overrides(fftoc_lib):
+    from fft_onchip_gb300 import onchip
+    sizes = (128, 256, 512)
+    before = {n: _lib.plan_query(n, _lib.ENGINE_FX)["variant"] for n in sizes}
+    try:
+        onchip.apply_plans("128:1,512:2", _lib.ENGINE_FX)
+        assert _lib.plan_query(128, _lib.ENGINE_FX)["variant"] == 1
+        assert _lib.plan_query(512, _lib.ENGINE_FX)["variant"] == 2
+        onchip.apply_plans("256:1")  # engine chosen per size
+        assert _lib.plan_query(256, fftoc_lib.fftoc_auto_engine(256))["variant"] == 1
+    finally:
+        for n, v in before.items():
+            _lib.plan_select(n, _lib.ENGINE_FX, v)
