@@ -50,3 +50,42 @@ def test_fx_conversion_round_trip(engine_report):
     # relative to the transform's largest element; an all-subnormal transform
     # loses a few bits (its largest exponent field is 0)
     assert engine_report["fx_roundtrip"] < 1e-13
+
+
+def _split_values():
+    """Edge and random values of the fixed-point range |x| < 2^61."""
+    import numpy as np
+    rng = np.random.default_rng(7)
+    lim = (1 << 61) - 1
+    edges = [0, 1, -1, lim, -lim, 1 << 30, -(1 << 30), (1 << 30) - 1, -(1 << 30) + 1, (1 << 60), -(1 << 60)]
+    edges += [k * (1 << 30) + d for k in (-3, -1, 0, 1, 5) for d in (-1, 0, 1)]
+    rand = rng.integers(-lim, lim, size=200000, dtype=np.int64, endpoint=True)
+    small = rng.integers(-(1 << 34), 1 << 34, size=50000, dtype=np.int64)
+    return np.concatenate([np.array(edges, dtype=np.int64), rand, small])
+
+
+def test_imad_split_low_limb_identity():
+    """The multiply-add form of the limb split (ImadSplit plans) computes
+    lo32(x) + xh * 0xC0000000 (mod 2^32) with xh = x >> 30; it must equal the
+    mask form x & (2^30 - 1), and xh must fit 32 bits."""
+    import numpy as np
+    x = _split_values()
+    xh = x >> 30                                            # arithmetic shift
+    assert xh.min() >= -(1 << 31) and xh.max() < (1 << 31)
+    lo32 = (x & 0xFFFFFFFF).astype(np.uint64)
+    xh32 = (xh & 0xFFFFFFFF).astype(np.uint64)
+    imad = (lo32 + xh32 * np.uint64(0xC0000000)) & np.uint64(0xFFFFFFFF)
+    mask = (x & ((1 << 30) - 1)).astype(np.uint64)
+    assert np.array_equal(imad, mask)
+    # and the limbs put x back together
+    assert np.array_equal(xh * (1 << 30) + mask.astype(np.int64), x)
+
+
+def test_out_hi_zero_test_matches_the_integer_test():
+    """OutHiZero plans test the high word of (double)x instead of x itself: a
+    nonzero integer converts to a double of magnitude >= 1, whose high word
+    is nonzero, and 0 converts to +0.0."""
+    import numpy as np
+    x = np.concatenate([_split_values(), np.array([np.iinfo(np.int64).min, np.iinfo(np.int64).max], dtype=np.int64)])
+    hi = (x.astype(np.float64).view(np.uint64) >> np.uint64(32)).astype(np.uint32)
+    assert np.array_equal(hi != 0, x != 0)
