@@ -116,6 +116,28 @@ static double check_conversions(std::mt19937_64& g) {
   return worst;
 }
 
+// The fast input conversion against the general one over the fast path's
+// domain: normal values whose exponent lies within 31 of eref (every size's
+// B, random signs, mantissas and exponents).  Returns the mismatch count.
+template <int NB>
+static double check_fx_in_near(std::mt19937_64& g) {
+  constexpr int B = FxBits<NB>::B;
+  long long bad = 0;
+  for (int trial = 0; trial < 200000; ++trial) {
+    const int em = 1 + (int)(g() % 2046);
+    const FxScale s = fx_scale<B>(em);
+    const int lo_e = s.eref - 31 > 1 ? s.eref - 31 : 1;
+    const int span = em - lo_e + 1;
+    if (span <= 0) continue;
+    const int e = lo_e + (int)(g() % (unsigned)span);
+    const unsigned long long bits = g();
+    const unsigned hw = (unsigned)(bits >> 32 & 0x800FFFFFu) | ((unsigned)e << 20);
+    const unsigned lw = (unsigned)bits;
+    if (fx_in_near(hw, lw, s.eref) != fx_in(hw, lw, s.eref)) ++bad;
+  }
+  return (double)bad;
+}
+
 int main() {
   std::mt19937_64 g(12345);
   printf("f64_dft2 %.3e\n", check_dft<EngF64, 2>(g, 1.0));
@@ -131,5 +153,6 @@ int main() {
   printf("fx_mulc_lsb %.3e\n", check_fx_mulc(g));
   const double r1 = check_conversions<4096>(g), r2 = check_conversions<16>(g);
   printf("fx_roundtrip %.3e\n", r1 > r2 ? r1 : r2);
+  printf("fx_in_near_mismatch %.0f\n", check_fx_in_near<8>(g) + check_fx_in_near<512>(g) + check_fx_in_near<4096>(g));
   return 0;
 }

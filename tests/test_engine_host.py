@@ -89,3 +89,9 @@ def test_out_hi_zero_test_matches_the_integer_test():
     x = np.concatenate([_split_values(), np.array([np.iinfo(np.int64).min, np.iinfo(np.int64).max], dtype=np.int64)])
     hi = (x.astype(np.float64).view(np.uint64) >> np.uint64(32)).astype(np.uint32)
     assert np.array_equal(hi != 0, x != 0)
+
+
+def test_fx_in_near_matches_fx_in_on_its_domain(engine_report):
+    # two funnel shifts instead of the 64-bit shift: bit-identical where the
+    # kernels take it (normal values within 2^31 of the transform maximum)
+    assert engine_report["fx_in_near_mismatch"] == 0
