@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <random>
 
 #include "fft_kernel.cuh"
@@ -138,6 +139,25 @@ static double check_fx_in_near(std::mt19937_64& g) {
   return (double)bad;
 }
 
+// The fast output conversion (exponent-field add, both zero tests) against
+// ldexp over values whose results stay normal, including zero.  Returns the
+// mismatch count.
+static double check_fx_out(std::mt19937_64& g) {
+  long long bad = 0;
+  for (int trial = 0; trial < 300000; ++trial) {
+    const int sh = (int)(g() % 62);
+    long long x = (long long)(g() >> (2 + sh));  // magnitudes 2^0 .. 2^62
+    if (g() & 1) x = -x;
+    if (trial % 1000 == 0) x = 0;
+    const int K = -1000 + (int)(g() % 1900);     // |x| 2^K within the normal range
+    const int kshift = (int)((unsigned)K << 20);
+    const double want = ldexp((double)x, K);
+    const double a = fx_out<false>(x, kshift), b = fx_out<true>(x, kshift);
+    if (memcmp(&a, &want, 8) != 0 || memcmp(&b, &want, 8) != 0) ++bad;
+  }
+  return (double)bad;
+}
+
 int main() {
   std::mt19937_64 g(12345);
   printf("f64_dft2 %.3e\n", check_dft<EngF64, 2>(g, 1.0));
@@ -154,5 +174,6 @@ int main() {
   const double r1 = check_conversions<4096>(g), r2 = check_conversions<16>(g);
   printf("fx_roundtrip %.3e\n", r1 > r2 ? r1 : r2);
   printf("fx_in_near_mismatch %.0f\n", check_fx_in_near<8>(g) + check_fx_in_near<512>(g) + check_fx_in_near<4096>(g));
+  printf("fx_out_mismatch %.0f\n", check_fx_out(g));
   return 0;
 }

@@ -95,3 +95,9 @@ def test_fx_in_near_matches_fx_in_on_its_domain(engine_report):
     # two funnel shifts instead of the 64-bit shift: bit-identical where the
     # kernels take it (normal values within 2^31 of the transform maximum)
     assert engine_report["fx_in_near_mismatch"] == 0
+
+
+def test_fx_out_matches_ldexp_in_the_normal_range(engine_report):
+    # (double)x with K added to its exponent field, zero tested on the integer
+    # or on the converted high word: the same bits as ldexp((double)x, K)
+    assert engine_report["fx_out_mismatch"] == 0
