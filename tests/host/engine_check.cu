@@ -158,6 +158,26 @@ static double check_fx_out(std::mt19937_64& g) {
   return (double)bad;
 }
 
+// The fixed-point constants of the DFT kernels: h*2^30 + l must be the
+// nearest integer to v*2^60, with 0 <= l < 2^30.  Returns the largest
+// distance from v*2^60 in units of the last place (at most 0.5), or 99 for a
+// low limb out of range.
+static double check_fx_konst() {
+  using K = Konst<EngFx>;
+  const long double pi = 3.141592653589793238462643383279502884L;
+  const long double r2 = sqrtl(0.5L), c8 = cosl(pi / 8), s8 = sinl(pi / 8);
+  const FxKC kc[] = {K::h(), K::nh(), K::c8(), K::s8(), K::nc8(), K::ns8()};
+  const long double v[] = {r2, -r2, c8, s8, -c8, -s8};
+  double worst = 0;
+  for (int i = 0; i < 6; ++i) {
+    if (kc[i].l < 0 || kc[i].l >= (1 << 30)) return 99;
+    const long double q = (long double)kc[i].h * 1073741824.0L + (long double)kc[i].l;
+    const double d = (double)fabsl(q - v[i] * 1152921504606846976.0L);
+    if (d > worst) worst = d;
+  }
+  return worst;
+}
+
 int main() {
   std::mt19937_64 g(12345);
   printf("f64_dft2 %.3e\n", check_dft<EngF64, 2>(g, 1.0));
@@ -175,5 +195,6 @@ int main() {
   printf("fx_roundtrip %.3e\n", r1 > r2 ? r1 : r2);
   printf("fx_in_near_mismatch %.0f\n", check_fx_in_near<8>(g) + check_fx_in_near<512>(g) + check_fx_in_near<4096>(g));
   printf("fx_out_mismatch %.0f\n", check_fx_out(g));
+  printf("fx_konst_ulp %.3f\n", check_fx_konst());
   return 0;
 }

@@ -101,3 +101,8 @@ def test_fx_out_matches_ldexp_in_the_normal_range(engine_report):
     # (double)x with K added to its exponent field, zero tested on the integer
     # or on the converted high word: the same bits as ldexp((double)x, K)
     assert engine_report["fx_out_mismatch"] == 0
+
+
+def test_fx_constants_are_rounded_limbs(engine_report):
+    # sqrt(1/2), cos(pi/8), sin(pi/8) and negatives as 30-bit limbs of v*2^60
+    assert engine_report["fx_konst_ulp"] <= 0.5
