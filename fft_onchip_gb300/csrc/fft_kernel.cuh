@@ -47,16 +47,22 @@ FFTOC_HD double from_words(unsigned hi, unsigned lo) {
 
 FFTOC_HD int expo_of(unsigned hw) { return (int)((hw >> 20) & 0x7FFu); }
 
-// value * 2^(1022 + B - Emax) truncated toward zero; eref = Emax + 53 - B.
+// value * 2^(1022 + B - Emax) rounded down (floor); eref = Emax + 53 - B.
+// With M the 53-bit significand and d = eref - e, a positive value gives
+// M >> d and a negative one ~(M >> d) = floor(-M / 2^d) - [2^d divides M]:
+// the complement of the shifted magnitude, which the fast path below forms
+// by complementing before the shift (one logic op per word instead of a
+// 64-bit negation).  Zeros of either sign give 0.
 FFTOC_HD long long fx_in(unsigned hw, unsigned lw, int eref) {
   const int e = expo_of(hw);
   const unsigned mh = (hw & 0xFFFFFu) | (e ? 0x100000u : 0u);
+  if ((mh | lw) == 0u) return 0;
   const int ee = e > 1 ? e : 1;
   const int d0 = eref - ee;
   const int d = d0 < 63 ? d0 : 63;
   const unsigned long long m = ((((unsigned long long)mh) << 32) | lw) >> d;
   const long long r = (long long)m;
-  return ((int)hw < 0) ? -r : r;
+  return ((int)hw < 0) ? ~r : r;
 }
 
 // x * 2^K, K = Emax - 1022 - B: the correctly rounded conversion with K added
@@ -107,33 +113,48 @@ FFTOC_HD FxScale fx_scale(int em) {
 }
 
 // Fast conversion for values within 2^31 of the transform's largest exponent
-// (all normal): (mantissa | implicit bit) >> d with d < 32 needs two funnel
-// shifts.  Bit-identical to fx_in for those values.
+// (all normal), bit-identical to fx_in there.  With S the sign mask
+// (0 or ~0), the 96-bit word S:(M ^ S) is shifted right by d with two
+// wrap-mode funnel shifts, which use d mod 32: d is taken as
+// eref - (hw >> 20), whose sign bit at position 11 is a multiple of 32.
 FFTOC_HD long long fx_in_near(unsigned hw, unsigned lw, int eref) {
-  const int d = eref - expo_of(hw);
-  const unsigned mh = (hw & 0xFFFFFu) | 0x100000u;
+  const unsigned S = (unsigned)((int)hw >> 31);
+  const unsigned mh = (hw & 0xFFFFFu) ^ (S ^ 0x100000u);  // ((hw & 0xFFFFF) | 0x100000) ^ S
+  const unsigned l = lw ^ S;
+  const unsigned d = (unsigned)eref - (hw >> 20);
 #ifdef __CUDA_ARCH__
-  const unsigned lo = __funnelshift_r(lw, mh, d);
+  unsigned lo, hi;
+  asm("shf.r.wrap.b32 %0, %1, %2, %3;" : "=r"(lo) : "r"(l), "r"(mh), "r"(d));
+  asm("shf.r.wrap.b32 %0, %1, %2, %3;" : "=r"(hi) : "r"(mh), "r"(S), "r"(d));
 #else
-  const unsigned lo = (unsigned)((((unsigned long long)mh << 32) | lw) >> d);
+  const unsigned sh = d & 31u;
+  const unsigned lo = (unsigned)((((unsigned long long)mh << 32) | l) >> sh);
+  const unsigned hi = (unsigned)((((unsigned long long)S << 32) | mh) >> sh);
 #endif
-  const unsigned hi = mh >> d;
-  const long long m = (long long)(((unsigned long long)hi << 32) | lo);
-  return ((int)hw < 0) ? -m : m;
+  return (long long)(((unsigned long long)hi << 32) | lo);
+}
+
+// Largest and smallest sign-cleared high words of a thread's raw points (the
+// biased exponent is the word >> 20).
+template <int P>
+FFTOC_HD void fx_word_range(const double2 (&raw)[P], unsigned& amax, unsigned& amin) {
+  amax = 0u;
+  amin = 0x7FFFFFFFu;
+#pragma unroll
+  for (int i = 0; i < P; ++i) {
+    const unsigned a = hi_word(raw[i].x) & 0x7FFFFFFFu, b = hi_word(raw[i].y) & 0x7FFFFFFFu;
+    const unsigned hi = a > b ? a : b, lo = a < b ? a : b;
+    amax = amax > hi ? amax : hi;
+    amin = amin < lo ? amin : lo;
+  }
 }
 
 // Convert a thread's P raw points; the fast path is taken when every value is
-// normal and within 2^31 of the transform maximum (the usual case).
+// normal and within 2^31 of the transform maximum (the usual case).  emin is
+// the thread's smallest biased exponent (fx_word_range).
 // OUTLINE: the other path calls the out-of-line fx_in_slow.
 template <int P, bool OUTLINE = false>
-FFTOC_HD void fx_convert_in(const double2 (&raw)[P], long long (&re)[P], long long (&im)[P], int eref) {
-  int emin = 0x7FF;
-#pragma unroll
-  for (int i = 0; i < P; ++i) {
-    const int a = expo_of(hi_word(raw[i].x)), b = expo_of(hi_word(raw[i].y));
-    emin = emin < a ? emin : a;
-    emin = emin < b ? emin : b;
-  }
+FFTOC_HD void fx_convert_in(const double2 (&raw)[P], long long (&re)[P], long long (&im)[P], int eref, int emin) {
   if (emin >= 1 && eref - emin < 32) {
 #pragma unroll
     for (int i = 0; i < P; ++i) {
@@ -154,6 +175,36 @@ FFTOC_HD void fx_convert_in(const double2 (&raw)[P], long long (&re)[P], long lo
     }
   }
 }
+template <int P, bool OUTLINE = false>
+FFTOC_HD void fx_convert_in(const double2 (&raw)[P], long long (&re)[P], long long (&im)[P], int eref) {
+  unsigned amax, amin;
+  fx_word_range<P>(raw, amax, amin);
+  fx_convert_in<P, OUTLINE>(raw, re, im, eref, (int)(amin >> 20));
+}
+
+// Largest value of em over the T consecutive threads of each transform (TPB
+// transforms per CTA, thread tid, transform j = tid / T).  T <= 32: within the
+// warp (a warp reduction for T = 32, shuffles over the T lanes otherwise).
+// T > 32 (whole warps per transform): a warp reduction, one word per warp in
+// `red` (TPB * T / 32 ints of shared memory) and one __syncthreads().
+template <int T, int TPB>
+__device__ __forceinline__ int fx_transform_max(int em, int tid, int j, int* red) {
+  if constexpr (T == 32) {
+    em = __reduce_max_sync(0xffffffffu, em);
+  } else if constexpr (T > 1 && T < 32) {
+#pragma unroll
+    for (int o = T / 2; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o, T));
+  } else if constexpr (T > 32) {
+    constexpr int W = T / 32;
+    em = __reduce_max_sync(0xffffffffu, em);
+    if ((tid & 31) == 0) red[tid >> 5] = em;
+    __syncthreads();
+    em = red[j * W];
+#pragma unroll
+    for (int w = 1; w < W; ++w) em = max(em, red[j * W + w]);
+  }
+  return em;
+}
 
 // --- the kernel ---------------------------------------------------------------
 template <class E, class PL>
@@ -172,7 +223,8 @@ struct Fft {
   static constexpr int NP = N + (N >> SH);
   static constexpr int THREADS = T * TPB;
   static constexpr bool STAGED = T < 8 && !PL::NO_STAGE;  // small N: stage HBM tiles through smem
-  static constexpr int SMEM = TPB * NP * 16 + 64;
+  static constexpr int SMEM = TPB * NP * 16 + 64;  // + 16 words of exponent scratch
+  static_assert(T <= 32 || TPB * (T / 32) <= 16, "exponent scratch holds one word per warp, 16 words");
 
   // 16-byte slot of element e of block-local transform j
   __device__ __forceinline__ static int slot(int j, int e) { return j * NP + e + (e >> SH); }
@@ -343,36 +395,22 @@ __device__ __forceinline__ void fft_tile(const Tile& tl, const typename E::TW* _
 
   S re[P], im[P];
   int K = 0, kshift = 0;
-  bool slow = false, special = false, slow_bits = false;
+  bool slow = false, special = false;
   if constexpr (E::kId == EngF64::kId) {
 #pragma unroll
     for (int i = 0; i < P; ++i) { re[i] = raw[i].x; im[i] = raw[i].y; }
   } else {
-    // largest biased exponent of the transform
-    int em = 0;
-#pragma unroll
-    for (int i = 0; i < P; ++i)
-      em = max(em, max(expo_of(hi_word(raw[i].x)), expo_of(hi_word(raw[i].y))));
-    if constexpr (T > 1 && T <= 32) {
-#pragma unroll
-      for (int o = T / 2; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o, T));
-    } else if constexpr (T > 32) {
-      // warps of one transform are contiguous: reduce per warp, then in smem
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
-      int* red = reinterpret_cast<int*>(smem_raw + TPB * F::NP * 16);
-      if (tid < TPB) red[tid] = 0;
-      __syncthreads();
-      if ((tid & 31) == 0) atomicMax(&red[j], em);
-      __syncthreads();
-      em = red[j];
-    }
+    // largest biased exponent of the transform, smallest of this thread
+    unsigned amax, amin;
+    fx_word_range<P>(raw, amax, amin);
+    const int em = fx_transform_max<T, TPB>((int)(amax >> 20), tid, j,
+                                            reinterpret_cast<int*>(smem_raw + TPB * F::NP * 16));
     const FxScale sc = fx_scale<FxBits<N>::B>(em);
     special = sc.special;
     K = sc.K;
     kshift = sc.kshift;
     slow = sc.slow;
-    fx_convert_in<P>(raw, re, im, sc.eref);
+    fx_convert_in<P>(raw, re, im, sc.eref, (int)(amin >> 20));
   }
 
   if constexpr (F::STAGED) __syncthreads();  // staging buffer is reused by the passes
@@ -381,38 +419,34 @@ __device__ __forceinline__ void fft_tile(const Tile& tl, const typename E::TW* _
   // ---- store: output m of butterfly b of the last pass is element dest(...)
   constexpr int RL = PL::R[NS - 1];
   constexpr int BL = P / RL;
-  auto result = [&](int i) -> double2 {
+  // Fixed point: the rare transforms whose outputs leave the normal range, or
+  // whose inputs were not finite, take the slow conversion (one branch per
+  // thread where the output goes straight to HBM, a select where it is staged).
+  auto value = [&](int i) -> double2 {
     if constexpr (E::kId == EngF64::kId) {
       return make_double2(re[i], im[i]);
     } else {
-      if (slow_bits) return make_double2(__longlong_as_double(re[i]), __longlong_as_double(im[i]));
       return make_double2(fx_out<PL::OUT_HI_ZERO>((long long)re[i], kshift),
                           fx_out<PL::OUT_HI_ZERO>((long long)im[i], kshift));
     }
   };
-  if constexpr (E::kId == EngFx::kId) {
-    // rare transforms (outputs outside the normal range, or non-finite
-    // inputs): convert in place on the slow path, then store as usual
-    if (slow || special) {
+  auto slow_value = [&](int i) -> double2 {
+    if constexpr (E::kId == EngF64::kId) {
+      return make_double2(re[i], im[i]);
+    } else {
       const double qnan = __longlong_as_double(0x7FF8000000000000LL);
-#pragma unroll
-      for (int i = 0; i < P; ++i) {
-        const double r = special ? qnan : fx_out_slow((long long)re[i], K);
-        const double m = special ? qnan : fx_out_slow((long long)im[i], K);
-        re[i] = __double_as_longlong(r);
-        im[i] = __double_as_longlong(m);
-      }
-      kshift = 0;
-      slow_bits = true;
+      return special ? make_double2(qnan, qnan)
+                     : make_double2(fx_out_slow((long long)re[i], K), fx_out_slow((long long)im[i], K));
     }
-  }
+  };
+  const bool redo = E::kId != EngF64::kId && (slow || special);
   if constexpr (F::STAGED) {
     if constexpr (NS > 1) __syncthreads();
 #pragma unroll
     for (int b = 0; b < BL; ++b)
 #pragma unroll
       for (int m = 0; m < RL; ++m) {
-        const double2 v = result(b + BL * m);
+        const double2 v = redo ? slow_value(b + BL * m) : value(b + BL * m);
         sm[F::slot(j, F::template dest<NS - 1>(t, b, m))] =
             make_longlong2(__double_as_longlong(v.x), __double_as_longlong(v.y));
       }
@@ -425,10 +459,17 @@ __device__ __forceinline__ void fft_tile(const Tile& tl, const typename E::TW* _
   } else {
     if (active) {
       double2* dst = tl.out_of(j);
+      if (!redo) {
 #pragma unroll
-      for (int b = 0; b < BL; ++b)
+        for (int b = 0; b < BL; ++b)
 #pragma unroll
-        for (int m = 0; m < RL; ++m) dst[F::template dest<NS - 1>(t, b, m)] = result(b + BL * m);
+          for (int m = 0; m < RL; ++m) dst[F::template dest<NS - 1>(t, b, m)] = value(b + BL * m);
+      } else {
+#pragma unroll
+        for (int b = 0; b < BL; ++b)
+#pragma unroll
+          for (int m = 0; m < RL; ++m) dst[F::template dest<NS - 1>(t, b, m)] = slow_value(b + BL * m);
+      }
     }
   }
 }
@@ -503,36 +544,22 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
 
   S re[P], im[P];
   int K = 0, kshift = 0;
-  bool slow = false, special = false, slow_bits = false;
+  bool slow = false, special = false;
   if constexpr (E::kId == EngF64::kId) {
 #pragma unroll
     for (int i = 0; i < P; ++i) { re[i] = raw[i].x; im[i] = raw[i].y; }
   } else {
-    // largest biased exponent of the transform
-    int em = 0;
-#pragma unroll
-    for (int i = 0; i < P; ++i)
-      em = max(em, max(expo_of(hi_word(raw[i].x)), expo_of(hi_word(raw[i].y))));
-    if constexpr (T > 1 && T <= 32) {
-#pragma unroll
-      for (int o = T / 2; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o, T));
-    } else if constexpr (T > 32) {
-      // warps of one transform are contiguous: reduce per warp, then in smem
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
-      int* red = reinterpret_cast<int*>(smem_raw + TPB * F::NP * 16);
-      if (tid < TPB) red[tid] = 0;
-      __syncthreads();
-      if ((tid & 31) == 0) atomicMax(&red[j], em);
-      __syncthreads();
-      em = red[j];
-    }
+    // largest biased exponent of the transform, smallest of this thread
+    unsigned amax, amin;
+    fx_word_range<P>(raw, amax, amin);
+    const int em = fx_transform_max<T, TPB>((int)(amax >> 20), tid, j,
+                                            reinterpret_cast<int*>(smem_raw + TPB * F::NP * 16));
     const FxScale sc = fx_scale<FxBits<N>::B>(em);
     special = sc.special;
     K = sc.K;
     kshift = sc.kshift;
     slow = sc.slow;
-    fx_convert_in<P, PL::OUTLINE_SLOW_IN>(raw, re, im, sc.eref);
+    fx_convert_in<P, PL::OUTLINE_SLOW_IN>(raw, re, im, sc.eref, (int)(amin >> 20));
   }
 
   if constexpr (F::STAGED) __syncthreads();  // staging buffer is reused by the passes
@@ -541,38 +568,34 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
   // ---- store: output m of butterfly b of the last pass is element dest(...)
   constexpr int RL = PL::R[NS - 1];
   constexpr int BL = P / RL;
-  auto result = [&](int i) -> double2 {
+  // Fixed point: the rare transforms whose outputs leave the normal range, or
+  // whose inputs were not finite, take the slow conversion (one branch per
+  // thread where the output goes straight to HBM, a select where it is staged).
+  auto value = [&](int i) -> double2 {
     if constexpr (E::kId == EngF64::kId) {
       return make_double2(re[i], im[i]);
     } else {
-      if (slow_bits) return make_double2(__longlong_as_double(re[i]), __longlong_as_double(im[i]));
       return make_double2(fx_out<PL::OUT_HI_ZERO>((long long)re[i], kshift),
                           fx_out<PL::OUT_HI_ZERO>((long long)im[i], kshift));
     }
   };
-  if constexpr (E::kId == EngFx::kId) {
-    // rare transforms (outputs outside the normal range, or non-finite
-    // inputs): convert in place on the slow path, then store as usual
-    if (slow || special) {
+  auto slow_value = [&](int i) -> double2 {
+    if constexpr (E::kId == EngF64::kId) {
+      return make_double2(re[i], im[i]);
+    } else {
       const double qnan = __longlong_as_double(0x7FF8000000000000LL);
-#pragma unroll
-      for (int i = 0; i < P; ++i) {
-        const double r = special ? qnan : fx_out_slow((long long)re[i], K);
-        const double m = special ? qnan : fx_out_slow((long long)im[i], K);
-        re[i] = __double_as_longlong(r);
-        im[i] = __double_as_longlong(m);
-      }
-      kshift = 0;
-      slow_bits = true;
+      return special ? make_double2(qnan, qnan)
+                     : make_double2(fx_out_slow((long long)re[i], K), fx_out_slow((long long)im[i], K));
     }
-  }
+  };
+  const bool redo = E::kId != EngF64::kId && (slow || special);
   if constexpr (F::STAGED) {
     if constexpr (NS > 1) __syncthreads();
 #pragma unroll
     for (int b = 0; b < BL; ++b)
 #pragma unroll
       for (int m = 0; m < RL; ++m) {
-        const double2 v = result(b + BL * m);
+        const double2 v = redo ? slow_value(b + BL * m) : value(b + BL * m);
         sm[F::slot(j, F::template dest<NS - 1>(t, b, m))] =
             make_longlong2(__double_as_longlong(v.x), __double_as_longlong(v.y));
       }
@@ -586,10 +609,17 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
   } else {
     if (active) {
       double2* dst = out + tr * N;
+      if (!redo) {
 #pragma unroll
-      for (int b = 0; b < BL; ++b)
+        for (int b = 0; b < BL; ++b)
 #pragma unroll
-        for (int m = 0; m < RL; ++m) dst[F::template dest<NS - 1>(t, b, m)] = result(b + BL * m);
+          for (int m = 0; m < RL; ++m) dst[F::template dest<NS - 1>(t, b, m)] = value(b + BL * m);
+      } else {
+#pragma unroll
+        for (int b = 0; b < BL; ++b)
+#pragma unroll
+          for (int m = 0; m < RL; ++m) dst[F::template dest<NS - 1>(t, b, m)] = slow_value(b + BL * m);
+      }
     }
   }
 }

@@ -70,7 +70,6 @@ struct Persist {
   static constexpr int BAR_OFF = RED_OFF + 64;
   static constexpr int SMEM = BAR_OFF + 8 * NSTAGE;
   static_assert(T >= 8, "pass-0 reads of the linear tile need >= 8 threads per transform");
-  static_assert(T <= 32 || TPB <= 16, "exponent scratch holds 16 transforms");
 };
 
 template <class E, class PL, int NSTAGE>
@@ -143,7 +142,7 @@ fft_fwd_persistent(const double2* __restrict__ in, double2* __restrict__ out, lo
     // pass-0 inputs from the linear tile: point i of this thread is element t + T*i
     S re[P], im[P];
     int K = 0, kshift = 0;
-    bool slow = false, special = false, slow_bits = false;
+    bool slow = false, special = false;
     if constexpr (E::kId == EngF64::kId) {
 #pragma unroll
       for (int i = 0; i < P; ++i) {
@@ -153,66 +152,57 @@ fft_fwd_persistent(const double2* __restrict__ in, double2* __restrict__ out, lo
       }
     } else {
       double2 raw[P];
-      int em = 0;
 #pragma unroll
       for (int i = 0; i < P; ++i) {
         const longlong2 v = active ? sm[j * N + t + T * i] : make_longlong2(0, 0);
         raw[i] = make_double2(__longlong_as_double(v.x), __longlong_as_double(v.y));
-        em = max(em, max(expo_of(hi_word(raw[i].x)), expo_of(hi_word(raw[i].y))));
       }
-      if constexpr (T <= 32) {
-#pragma unroll
-        for (int o = T / 2; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o, T));
-      } else {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
-        if (tid < TPB) red[tid] = 0;
-        __syncthreads();
-        if ((tid & 31) == 0) atomicMax(&red[j], em);
-        __syncthreads();
-        em = red[j];
-      }
+      unsigned amax, amin;
+      fx_word_range<P>(raw, amax, amin);
+      const int em = fx_transform_max<T, TPB>((int)(amax >> 20), tid, j, red);
       const FxScale sc = fx_scale<FxBits<N>::B>(em);
       special = sc.special;
       K = sc.K;
       kshift = sc.kshift;
       slow = sc.slow;
-      fx_convert_in<P>(raw, re, im, sc.eref);
+      fx_convert_in<P>(raw, re, im, sc.eref, (int)(amin >> 20));
     }
     if constexpr (NS > 1) __syncthreads();  // every linear read is done before pass-0 writes
     F::template run_passes<0>(re, im, j, t, tw, sm);
 
-    if constexpr (E::kId == EngFx::kId) {
-      if (slow || special) {
-        const double qnan = __longlong_as_double(0x7FF8000000000000LL);
-#pragma unroll
-        for (int i = 0; i < P; ++i) {
-          const double r = special ? qnan : fx_out_slow((long long)re[i], K);
-          const double m = special ? qnan : fx_out_slow((long long)im[i], K);
-          re[i] = __double_as_longlong(r);
-          im[i] = __double_as_longlong(m);
-        }
-        slow_bits = true;
-      }
-    }
+    // fixed point: one branch per thread between the fast conversion and, for
+    // the rare transforms whose outputs leave the normal range (or had
+    // non-finite inputs), the slow one
     constexpr int RL = PL::R[NS - 1];
     constexpr int BL = P / RL;
     if (active) {
       double2* dst = out + tr * N;
+      if (E::kId == EngF64::kId || !(slow || special)) {
 #pragma unroll
-      for (int b = 0; b < BL; ++b)
+        for (int b = 0; b < BL; ++b)
 #pragma unroll
-        for (int m = 0; m < RL; ++m) {
-          const int i = b + BL * m;
-          double2 v;
-          if constexpr (E::kId == EngF64::kId) {
-            v = make_double2(re[i], im[i]);
-          } else {
-            v = slow_bits ? make_double2(__longlong_as_double(re[i]), __longlong_as_double(im[i]))
-                          : make_double2(fx_out((long long)re[i], kshift), fx_out((long long)im[i], kshift));
+          for (int m = 0; m < RL; ++m) {
+            const int i = b + BL * m;
+            double2 v;
+            if constexpr (E::kId == EngF64::kId) {
+              v = make_double2(re[i], im[i]);
+            } else {
+              v = make_double2(fx_out((long long)re[i], kshift), fx_out((long long)im[i], kshift));
+            }
+            dst[F::template dest<NS - 1>(t, b, m)] = v;
           }
-          dst[F::template dest<NS - 1>(t, b, m)] = v;
-        }
+      } else {
+        const double qnan = __longlong_as_double(0x7FF8000000000000LL);
+#pragma unroll
+        for (int b = 0; b < BL; ++b)
+#pragma unroll
+          for (int m = 0; m < RL; ++m) {
+            const int i = b + BL * m;
+            dst[F::template dest<NS - 1>(t, b, m)] =
+                special ? make_double2(qnan, qnan)
+                        : make_double2(fx_out_slow((long long)re[i], K), fx_out_slow((long long)im[i], K));
+          }
+      }
     }
     // this thread's generic-proxy writes to stage s are ordered before the
     // bulk copy that refills it (async proxy) after the barrier

@@ -44,7 +44,7 @@ struct KernelDesc {
   int smem_onchip = 0;
 };
 
-constexpr int kMaxVariants = 8;
+constexpr int kMaxVariants = 12;
 struct SizeVariants {
   int count = 0;
   KernelDesc v[kMaxVariants];

@@ -114,29 +114,17 @@ struct fft {
 #pragma unroll
       for (int i = 0; i < P; ++i) { re[i] = raw[i].x; im[i] = raw[i].y; }
     } else {
-      int em = 0;  // largest biased exponent of the transform
-#pragma unroll
-      for (int i = 0; i < P; ++i)
-        em = max(em, max(expo_of(hi_word(raw[i].x)), expo_of(hi_word(raw[i].y))));
-      if constexpr (T > 1 && T <= 32) {
-#pragma unroll
-        for (int o = T / 2; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o, T));
-      } else if constexpr (T > 32) {
-        __shared__ int red[transforms_per_block];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
-        if (tid < transforms_per_block) red[tid] = 0;
-        __syncthreads();
-        if ((tid & 31) == 0) atomicMax(&red[j], em);
-        __syncthreads();
-        em = red[j];
-      }
+      // largest biased exponent of the transform, smallest of this thread
+      __shared__ int red[transforms_per_block * (T > 32 ? T / 32 : 1)];
+      unsigned amax, amin;
+      fx_word_range<P>(raw, amax, amin);
+      const int em = fx_transform_max<T, transforms_per_block>((int)(amax >> 20), tid, j, red);
       const FxScale sc = fx_scale<FxBits<Size>::B>(em);
       special = sc.special;
       K = sc.K;
       kshift = sc.kshift;
       slow = sc.slow;
-      fx_convert_in<P>(raw, re, im, sc.eref);
+      fx_convert_in<P>(raw, re, im, sc.eref, (int)(amin >> 20));
     }
     __syncthreads();  // the whole tile is in registers: it is the exchange area from here on
 
