@@ -15,6 +15,19 @@ template <int N> struct FxBits {
   static constexpr int B = (61 - ilog2c(N)) < 53 ? (61 - ilog2c(N)) : 53;
 };
 
+// Rounding of the binary64 -> fixed-point input conversion of a size N.
+// Small transforms (N <= 32) stream at the HBM limit with every resident CTA
+// slot in use; there the truncating sequence (round toward zero, a negation
+// after the shift) fits 64 registers and measured fastest (+9% at N = 8 on
+// GB300).  From N = 64 up the kernels are bound by the integer pipes, and the
+// floor sequence (the sign complemented before the shift, fewer instructions)
+// measured 1-5% faster.  Every path of one size (batched, uneven, on-chip,
+// device executors) uses its size's rounding, so their results agree bit for
+// bit.
+template <int N> struct FxTrunc {
+  static constexpr bool value = N <= 32;
+};
+
 // --- binary64 <-> block fixed point -------------------------------------------
 FFTOC_HD unsigned hi_word(double v) {
 #ifdef __CUDA_ARCH__
@@ -47,12 +60,13 @@ FFTOC_HD double from_words(unsigned hi, unsigned lo) {
 
 FFTOC_HD int expo_of(unsigned hw) { return (int)((hw >> 20) & 0x7FFu); }
 
-// value * 2^(1022 + B - Emax) rounded down (floor); eref = Emax + 53 - B.
-// With M the 53-bit significand and d = eref - e, a positive value gives
-// M >> d and a negative one ~(M >> d) = floor(-M / 2^d) - [2^d divides M]:
-// the complement of the shifted magnitude, which the fast path below forms
-// by complementing before the shift (one logic op per word instead of a
-// 64-bit negation).  Zeros of either sign give 0.
+// value * 2^(1022 + B - Emax), eref = Emax + 53 - B, with M the 53-bit
+// significand and d = eref - e: M >> d for a positive value.  A negative one
+// gives -(M >> d) (TRUNC: toward zero) or ~(M >> d) = floor(-M / 2^d) -
+// [2^d divides M] (floor: the complement of the shifted magnitude, which the
+// fast path below forms by complementing before the shift).  Zeros of either
+// sign give 0.
+template <bool TRUNC = false>
 FFTOC_HD long long fx_in(unsigned hw, unsigned lw, int eref) {
   const int e = expo_of(hw);
   const unsigned mh = (hw & 0xFFFFFu) | (e ? 0x100000u : 0u);
@@ -62,7 +76,7 @@ FFTOC_HD long long fx_in(unsigned hw, unsigned lw, int eref) {
   const int d = d0 < 63 ? d0 : 63;
   const unsigned long long m = ((((unsigned long long)mh) << 32) | lw) >> d;
   const long long r = (long long)m;
-  return ((int)hw < 0) ? ~r : r;
+  return ((int)hw < 0) ? (TRUNC ? -r : ~r) : r;
 }
 
 // x * 2^K, K = Emax - 1022 - B: the correctly rounded conversion with K added
@@ -89,9 +103,11 @@ inline double fx_out_slow(long long x, int K) { return ldexp((double)x, K); }
 
 // fx_in out of line, for the rare transforms that leave the fast input path.
 #ifdef __CUDA_ARCH__
-__device__ __noinline__ long long fx_in_slow(unsigned hw, unsigned lw, int eref) { return fx_in(hw, lw, eref); }
+template <bool TRUNC>
+__device__ __noinline__ long long fx_in_slow(unsigned hw, unsigned lw, int eref) { return fx_in<TRUNC>(hw, lw, eref); }
 #else
-inline long long fx_in_slow(unsigned hw, unsigned lw, int eref) { return fx_in(hw, lw, eref); }
+template <bool TRUNC>
+inline long long fx_in_slow(unsigned hw, unsigned lw, int eref) { return fx_in<TRUNC>(hw, lw, eref); }
 #endif
 
 // Scale parameters of a transform from its largest biased exponent.
@@ -134,52 +150,93 @@ FFTOC_HD long long fx_in_near(unsigned hw, unsigned lw, int eref) {
   return (long long)(((unsigned long long)hi << 32) | lo);
 }
 
-// Largest and smallest sign-cleared high words of a thread's raw points (the
-// biased exponent is the word >> 20).
-template <int P>
-FFTOC_HD void fx_word_range(const double2 (&raw)[P], unsigned& amax, unsigned& amin) {
-  amax = 0u;
-  amin = 0x7FFFFFFFu;
+// The truncating fast conversion (bit-identical to fx_in<true> on the same
+// domain): the shifted magnitude, negated for a negative value.
+FFTOC_HD long long fx_in_near_trunc(unsigned hw, unsigned lw, int eref) {
+  const int d = eref - expo_of(hw);
+  const unsigned mh = (hw & 0xFFFFFu) | 0x100000u;
+#ifdef __CUDA_ARCH__
+  const unsigned lo = __funnelshift_r(lw, mh, d);
+#else
+  const unsigned lo = (unsigned)((((unsigned long long)mh << 32) | lw) >> d);
+#endif
+  const unsigned hi = mh >> d;
+  const long long m = (long long)(((unsigned long long)hi << 32) | lo);
+  return ((int)hw < 0) ? -m : m;
+}
+
+// Largest and smallest biased exponents of a thread's raw points: from the
+// sign-cleared high words (floor sizes), or the exponent fields in two loops
+// (the sequence that fits the small sizes' register budget).
+template <int P, bool TRUNC = false>
+FFTOC_HD void fx_exponent_range(const double2 (&raw)[P], int& emax, int& emin) {
+  if constexpr (TRUNC) {
+    int em = 0, en = 0x7FF;
 #pragma unroll
-  for (int i = 0; i < P; ++i) {
-    const unsigned a = hi_word(raw[i].x) & 0x7FFFFFFFu, b = hi_word(raw[i].y) & 0x7FFFFFFFu;
-    const unsigned hi = a > b ? a : b, lo = a < b ? a : b;
-    amax = amax > hi ? amax : hi;
-    amin = amin < lo ? amin : lo;
+    for (int i = 0; i < P; ++i) {
+      const int a = expo_of(hi_word(raw[i].x)), b = expo_of(hi_word(raw[i].y));
+      const int hi = a > b ? a : b;
+      em = em > hi ? em : hi;
+    }
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      const int a = expo_of(hi_word(raw[i].x)), b = expo_of(hi_word(raw[i].y));
+      en = en < a ? en : a;
+      en = en < b ? en : b;
+    }
+    emax = em;
+    emin = en;
+  } else {
+    unsigned amax = 0u, amin = 0x7FFFFFFFu;
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      const unsigned a = hi_word(raw[i].x) & 0x7FFFFFFFu, b = hi_word(raw[i].y) & 0x7FFFFFFFu;
+      const unsigned hi = a > b ? a : b, lo = a < b ? a : b;
+      amax = amax > hi ? amax : hi;
+      amin = amin < lo ? amin : lo;
+    }
+    emax = (int)(amax >> 20);
+    emin = (int)(amin >> 20);
   }
 }
 
 // Convert a thread's P raw points; the fast path is taken when every value is
 // normal and within 2^31 of the transform maximum (the usual case).  emin is
-// the thread's smallest biased exponent (fx_word_range).
-// OUTLINE: the other path calls the out-of-line fx_in_slow.
-template <int P, bool OUTLINE = false>
+// the thread's smallest biased exponent (fx_exponent_range).
+// OUTLINE: the other path calls the out-of-line fx_in_slow.  TRUNC: the
+// size's rounding (FxTrunc).
+template <int P, bool OUTLINE = false, bool TRUNC = false>
 FFTOC_HD void fx_convert_in(const double2 (&raw)[P], long long (&re)[P], long long (&im)[P], int eref, int emin) {
   if (emin >= 1 && eref - emin < 32) {
 #pragma unroll
     for (int i = 0; i < P; ++i) {
-      re[i] = fx_in_near(hi_word(raw[i].x), lo_word(raw[i].x), eref);
-      im[i] = fx_in_near(hi_word(raw[i].y), lo_word(raw[i].y), eref);
+      if constexpr (TRUNC) {
+        re[i] = fx_in_near_trunc(hi_word(raw[i].x), lo_word(raw[i].x), eref);
+        im[i] = fx_in_near_trunc(hi_word(raw[i].y), lo_word(raw[i].y), eref);
+      } else {
+        re[i] = fx_in_near(hi_word(raw[i].x), lo_word(raw[i].x), eref);
+        im[i] = fx_in_near(hi_word(raw[i].y), lo_word(raw[i].y), eref);
+      }
     }
   } else if constexpr (OUTLINE) {
 #pragma unroll
     for (int i = 0; i < P; ++i) {
-      re[i] = fx_in_slow(hi_word(raw[i].x), lo_word(raw[i].x), eref);
-      im[i] = fx_in_slow(hi_word(raw[i].y), lo_word(raw[i].y), eref);
+      re[i] = fx_in_slow<TRUNC>(hi_word(raw[i].x), lo_word(raw[i].x), eref);
+      im[i] = fx_in_slow<TRUNC>(hi_word(raw[i].y), lo_word(raw[i].y), eref);
     }
   } else {
 #pragma unroll
     for (int i = 0; i < P; ++i) {
-      re[i] = fx_in(hi_word(raw[i].x), lo_word(raw[i].x), eref);
-      im[i] = fx_in(hi_word(raw[i].y), lo_word(raw[i].y), eref);
+      re[i] = fx_in<TRUNC>(hi_word(raw[i].x), lo_word(raw[i].x), eref);
+      im[i] = fx_in<TRUNC>(hi_word(raw[i].y), lo_word(raw[i].y), eref);
     }
   }
 }
-template <int P, bool OUTLINE = false>
+template <int P, bool OUTLINE = false, bool TRUNC = false>
 FFTOC_HD void fx_convert_in(const double2 (&raw)[P], long long (&re)[P], long long (&im)[P], int eref) {
-  unsigned amax, amin;
-  fx_word_range<P>(raw, amax, amin);
-  fx_convert_in<P, OUTLINE>(raw, re, im, eref, (int)(amin >> 20));
+  int emax, emin;
+  fx_exponent_range<P, TRUNC>(raw, emax, emin);
+  fx_convert_in<P, OUTLINE, TRUNC>(raw, re, im, eref, emin);
 }
 
 // Largest value of em over the T consecutive threads of each transform (TPB
@@ -401,16 +458,16 @@ __device__ __forceinline__ void fft_tile(const Tile& tl, const typename E::TW* _
     for (int i = 0; i < P; ++i) { re[i] = raw[i].x; im[i] = raw[i].y; }
   } else {
     // largest biased exponent of the transform, smallest of this thread
-    unsigned amax, amin;
-    fx_word_range<P>(raw, amax, amin);
-    const int em = fx_transform_max<T, TPB>((int)(amax >> 20), tid, j,
-                                            reinterpret_cast<int*>(smem_raw + TPB * F::NP * 16));
+    constexpr bool TR = FxTrunc<N>::value;
+    int em, emin;
+    fx_exponent_range<P, TR>(raw, em, emin);
+    em = fx_transform_max<T, TPB>(em, tid, j, reinterpret_cast<int*>(smem_raw + TPB * F::NP * 16));
     const FxScale sc = fx_scale<FxBits<N>::B>(em);
     special = sc.special;
     K = sc.K;
     kshift = sc.kshift;
     slow = sc.slow;
-    fx_convert_in<P>(raw, re, im, sc.eref, (int)(amin >> 20));
+    fx_convert_in<P, false, TR>(raw, re, im, sc.eref, emin);
   }
 
   if constexpr (F::STAGED) __syncthreads();  // staging buffer is reused by the passes
@@ -420,8 +477,9 @@ __device__ __forceinline__ void fft_tile(const Tile& tl, const typename E::TW* _
   constexpr int RL = PL::R[NS - 1];
   constexpr int BL = P / RL;
   // Fixed point: the rare transforms whose outputs leave the normal range, or
-  // whose inputs were not finite, take the slow conversion (one branch per
-  // thread where the output goes straight to HBM, a select where it is staged).
+  // whose inputs were not finite, take the slow conversion: a per-value select
+  // where the output is staged or the size is small (FxTrunc; both measured
+  // faster so), else one branch per thread between two store loops.
   auto value = [&](int i) -> double2 {
     if constexpr (E::kId == EngF64::kId) {
       return make_double2(re[i], im[i]);
@@ -440,13 +498,34 @@ __device__ __forceinline__ void fft_tile(const Tile& tl, const typename E::TW* _
     }
   };
   const bool redo = E::kId != EngF64::kId && (slow || special);
+  // Small sizes with at most 4 points per thread: the slow values replace the
+  // fixed-point words in place (one branch; the words are few, so this costs
+  // no registers), and the stores select the words or the fast conversion.
+  constexpr bool IN_PLACE = E::kId != EngF64::kId && FxTrunc<N>::value && P <= 4;
+  if constexpr (IN_PLACE) {
+    if (redo) {
+#pragma unroll
+      for (int i = 0; i < P; ++i) {
+        const double2 v = slow_value(i);
+        re[i] = __double_as_longlong(v.x);
+        im[i] = __double_as_longlong(v.y);
+      }
+    }
+  }
+  auto stored = [&](int i) -> double2 {
+    if constexpr (IN_PLACE) {
+      return redo ? make_double2(__longlong_as_double(re[i]), __longlong_as_double(im[i])) : value(i);
+    } else {
+      return redo ? slow_value(i) : value(i);
+    }
+  };
   if constexpr (F::STAGED) {
     if constexpr (NS > 1) __syncthreads();
 #pragma unroll
     for (int b = 0; b < BL; ++b)
 #pragma unroll
       for (int m = 0; m < RL; ++m) {
-        const double2 v = redo ? slow_value(b + BL * m) : value(b + BL * m);
+        const double2 v = stored(b + BL * m);
         sm[F::slot(j, F::template dest<NS - 1>(t, b, m))] =
             make_longlong2(__double_as_longlong(v.x), __double_as_longlong(v.y));
       }
@@ -459,7 +538,13 @@ __device__ __forceinline__ void fft_tile(const Tile& tl, const typename E::TW* _
   } else {
     if (active) {
       double2* dst = tl.out_of(j);
-      if (!redo) {
+      if constexpr (FxTrunc<N>::value) {
+#pragma unroll
+        for (int b = 0; b < BL; ++b)
+#pragma unroll
+          for (int m = 0; m < RL; ++m)
+            dst[F::template dest<NS - 1>(t, b, m)] = stored(b + BL * m);
+      } else if (!redo) {
 #pragma unroll
         for (int b = 0; b < BL; ++b)
 #pragma unroll
@@ -550,16 +635,16 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
     for (int i = 0; i < P; ++i) { re[i] = raw[i].x; im[i] = raw[i].y; }
   } else {
     // largest biased exponent of the transform, smallest of this thread
-    unsigned amax, amin;
-    fx_word_range<P>(raw, amax, amin);
-    const int em = fx_transform_max<T, TPB>((int)(amax >> 20), tid, j,
-                                            reinterpret_cast<int*>(smem_raw + TPB * F::NP * 16));
+    constexpr bool TR = FxTrunc<N>::value;
+    int em, emin;
+    fx_exponent_range<P, TR>(raw, em, emin);
+    em = fx_transform_max<T, TPB>(em, tid, j, reinterpret_cast<int*>(smem_raw + TPB * F::NP * 16));
     const FxScale sc = fx_scale<FxBits<N>::B>(em);
     special = sc.special;
     K = sc.K;
     kshift = sc.kshift;
     slow = sc.slow;
-    fx_convert_in<P, PL::OUTLINE_SLOW_IN>(raw, re, im, sc.eref, (int)(amin >> 20));
+    fx_convert_in<P, PL::OUTLINE_SLOW_IN, TR>(raw, re, im, sc.eref, emin);
   }
 
   if constexpr (F::STAGED) __syncthreads();  // staging buffer is reused by the passes
@@ -569,8 +654,9 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
   constexpr int RL = PL::R[NS - 1];
   constexpr int BL = P / RL;
   // Fixed point: the rare transforms whose outputs leave the normal range, or
-  // whose inputs were not finite, take the slow conversion (one branch per
-  // thread where the output goes straight to HBM, a select where it is staged).
+  // whose inputs were not finite, take the slow conversion: a per-value select
+  // where the output is staged or the size is small (FxTrunc; both measured
+  // faster so), else one branch per thread between two store loops.
   auto value = [&](int i) -> double2 {
     if constexpr (E::kId == EngF64::kId) {
       return make_double2(re[i], im[i]);
@@ -589,13 +675,34 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
     }
   };
   const bool redo = E::kId != EngF64::kId && (slow || special);
+  // Small sizes with at most 4 points per thread: the slow values replace the
+  // fixed-point words in place (one branch; the words are few, so this costs
+  // no registers), and the stores select the words or the fast conversion.
+  constexpr bool IN_PLACE = E::kId != EngF64::kId && FxTrunc<N>::value && P <= 4;
+  if constexpr (IN_PLACE) {
+    if (redo) {
+#pragma unroll
+      for (int i = 0; i < P; ++i) {
+        const double2 v = slow_value(i);
+        re[i] = __double_as_longlong(v.x);
+        im[i] = __double_as_longlong(v.y);
+      }
+    }
+  }
+  auto stored = [&](int i) -> double2 {
+    if constexpr (IN_PLACE) {
+      return redo ? make_double2(__longlong_as_double(re[i]), __longlong_as_double(im[i])) : value(i);
+    } else {
+      return redo ? slow_value(i) : value(i);
+    }
+  };
   if constexpr (F::STAGED) {
     if constexpr (NS > 1) __syncthreads();
 #pragma unroll
     for (int b = 0; b < BL; ++b)
 #pragma unroll
       for (int m = 0; m < RL; ++m) {
-        const double2 v = redo ? slow_value(b + BL * m) : value(b + BL * m);
+        const double2 v = stored(b + BL * m);
         sm[F::slot(j, F::template dest<NS - 1>(t, b, m))] =
             make_longlong2(__double_as_longlong(v.x), __double_as_longlong(v.y));
       }
@@ -609,7 +716,13 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
   } else {
     if (active) {
       double2* dst = out + tr * N;
-      if (!redo) {
+      if constexpr (FxTrunc<N>::value) {
+#pragma unroll
+        for (int b = 0; b < BL; ++b)
+#pragma unroll
+          for (int m = 0; m < RL; ++m)
+            dst[F::template dest<NS - 1>(t, b, m)] = stored(b + BL * m);
+      } else if (!redo) {
 #pragma unroll
         for (int b = 0; b < BL; ++b)
 #pragma unroll

@@ -157,15 +157,16 @@ fft_fwd_persistent(const double2* __restrict__ in, double2* __restrict__ out, lo
         const longlong2 v = active ? sm[j * N + t + T * i] : make_longlong2(0, 0);
         raw[i] = make_double2(__longlong_as_double(v.x), __longlong_as_double(v.y));
       }
-      unsigned amax, amin;
-      fx_word_range<P>(raw, amax, amin);
-      const int em = fx_transform_max<T, TPB>((int)(amax >> 20), tid, j, red);
+      constexpr bool TR = FxTrunc<N>::value;
+      int em, emin;
+      fx_exponent_range<P, TR>(raw, em, emin);
+      em = fx_transform_max<T, TPB>(em, tid, j, red);
       const FxScale sc = fx_scale<FxBits<N>::B>(em);
       special = sc.special;
       K = sc.K;
       kshift = sc.kshift;
       slow = sc.slow;
-      fx_convert_in<P>(raw, re, im, sc.eref, (int)(amin >> 20));
+      fx_convert_in<P, false, TR>(raw, re, im, sc.eref, emin);
     }
     if constexpr (NS > 1) __syncthreads();  // every linear read is done before pass-0 writes
     F::template run_passes<0>(re, im, j, t, tw, sm);

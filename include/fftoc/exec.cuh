@@ -116,15 +116,16 @@ struct fft {
     } else {
       // largest biased exponent of the transform, smallest of this thread
       __shared__ int red[transforms_per_block * (T > 32 ? T / 32 : 1)];
-      unsigned amax, amin;
-      fx_word_range<P>(raw, amax, amin);
-      const int em = fx_transform_max<T, transforms_per_block>((int)(amax >> 20), tid, j, red);
+      constexpr bool TR = FxTrunc<Size>::value;
+      int em, emin;
+      fx_exponent_range<P, TR>(raw, em, emin);
+      em = fx_transform_max<T, transforms_per_block>(em, tid, j, red);
       const FxScale sc = fx_scale<FxBits<Size>::B>(em);
       special = sc.special;
       K = sc.K;
       kshift = sc.kshift;
       slow = sc.slow;
-      fx_convert_in<P>(raw, re, im, sc.eref, (int)(amin >> 20));
+      fx_convert_in<P, false, TR>(raw, re, im, sc.eref, emin);
     }
     __syncthreads();  // the whole tile is in registers: it is the exchange area from here on
 

@@ -117,8 +117,8 @@ static double check_conversions(std::mt19937_64& g) {
   return worst;
 }
 
-// The fast input conversion against the general one over the fast path's
-// domain: normal values whose exponent lies within 31 of eref (every size's
+// The fast input conversions (floor and truncating) against the general one
+// of the same rounding over the fast path's domain: normal values whose exponent lies within 31 of eref (every size's
 // B, random signs, mantissas and exponents).  Returns the mismatch count.
 template <int NB>
 static double check_fx_in_near(std::mt19937_64& g) {
@@ -134,7 +134,8 @@ static double check_fx_in_near(std::mt19937_64& g) {
     const unsigned long long bits = g();
     const unsigned hw = (unsigned)(bits >> 32 & 0x800FFFFFu) | ((unsigned)e << 20);
     const unsigned lw = (unsigned)bits;
-    if (fx_in_near(hw, lw, s.eref) != fx_in(hw, lw, s.eref)) ++bad;
+    if (fx_in_near(hw, lw, s.eref) != fx_in<false>(hw, lw, s.eref)) ++bad;
+    if (fx_in_near_trunc(hw, lw, s.eref) != fx_in<true>(hw, lw, s.eref)) ++bad;
   }
   return (double)bad;
 }
