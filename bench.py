@@ -52,13 +52,13 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=1.5, help="CPU-baseline sample time per size")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU-baseline time of the all-threads leg")
     ap.add_argument("--gib", type=float, default=1.0, help="input GiB per size (1.0 = the sweep configuration)")
     ap.add_argument("--plan", default="", help="N:variant,... plan overrides (default: the library's choice)")
     ap.add_argument("--tuning", default="", help="tuning JSON written by fft_onchip_gb300.tune to apply")
-    ap.add_argument("--forms", default="split,uneven,serve,onchip,cufft",
-                    help="extra workloads measured after the sweep (comma list of: split, uneven, serve, onchip, "
-                         "cufft; empty for none)")
+    ap.add_argument("--forms", default="config1,split,uneven,serve,onchip,cufft",
+                    help="extra workloads measured after the sweep (comma list of: config1, split, uneven, serve, "
+                         "onchip, cufft; empty for none)")
     ap.add_argument("--serve-rates", default="1e3,1e4,1e5,1e6", help="offered request rates (req/s) of the serving loop")
     ap.add_argument("--uneven-count", type=int, default=200000)
     return ap.parse_args()
@@ -177,35 +177,44 @@ def _timed(fn, x, seconds):
             return reps * x.shape[0], el
 
 
-def cpu_sample_rate(sizes, seconds_per_size):
+def cpu_sample_rate(sizes, seconds):
     """The port on all host threads (the baseline), plus two secondary points
     on the same samples: the port on one thread and numpy.fft (pocketfft,
-    one thread).  Each is FFT/s over the sweep (transforms / summed time)."""
+    one thread).  Each size's sample is 1/64 of its 1 GiB batch, and every
+    round runs each sample once, so the per-size weighting is the GPU
+    `value`'s (transforms in proportion to 1 GiB / (16 N)); rounds repeat
+    until the leg has run `seconds` (the 1-thread legs a third of it).
+    Each leg's figure is FFT/s over the sweep (transforms / summed time)."""
     import numpy as np
     from fft_onchip_gb300 import inputs
     from oracle import oracle as O
     threads = O.max_threads()
-    legs = {"all": (lambda x: O.fft_f64(x, threads=0), seconds_per_size),
-            "one": (lambda x: O.fft_f64(x, threads=1), seconds_per_size / 3),
-            "numpy": (lambda x: np.fft.fft(x, axis=1), seconds_per_size / 3)}
-    acc = {k: [0, 0.0, {}] for k in legs}
-    for n in sizes:
-        batch = (GIB // (16 * n))
-        sample = max(1, batch // 64)
-        x = inputs.normal(n, sample, seed=n)
-        O.fft_f64(x[: max(1, sample // 16)], threads=0)  # warm the pool and caches
-        for k, (fn, sec) in legs.items():
-            f, el = _timed(fn, x, sec)
-            acc[k][0] += f
-            acc[k][1] += el
-            acc[k][2][str(n)] = f / el
-    rate = {k: v[0] / v[1] for k, v in acc.items()}
-    return rate["all"], threads, acc["all"][2], {
+    samples = {n: inputs.normal(n, max(1, (GIB // (16 * n)) // 64), seed=n) for n in sizes}
+    for n in sizes:  # warm the pool and caches
+        O.fft_f64(samples[n][: max(1, samples[n].shape[0] // 16)], threads=0)
+    legs = {"all": (lambda x: O.fft_f64(x, threads=0), seconds),
+            "one": (lambda x: O.fft_f64(x, threads=1), seconds / 3),
+            "numpy": (lambda x: np.fft.fft(x, axis=1), seconds / 3)}
+    res = {}
+    for k, (fn, sec) in legs.items():
+        ffts, el, per, rounds = 0, 0.0, {n: [0, 0.0] for n in sizes}, 0
+        while rounds == 0 or el < sec:
+            for n in sizes:
+                t0 = time.perf_counter()
+                fn(samples[n])
+                dt = time.perf_counter() - t0
+                ffts += samples[n].shape[0]
+                el += dt
+                per[n][0] += samples[n].shape[0]
+                per[n][1] += dt
+            rounds += 1
+        res[k] = (ffts / el, {str(n): round(v[0] / v[1], 1) for n, v in per.items()}, rounds)
+    return res["all"][0], threads, res["all"][1], {
+        "rounds": res["all"][2],
         "nproc": os.cpu_count(),
-        "one_core": {"value": rate["one"], "cores": 1,
-                     "per_n": {k: round(v, 1) for k, v in acc["one"][2].items()}},
-        "numpy_fft": {"value": rate["numpy"], "cores": 1, "what": "numpy.fft.fft (pocketfft) on the same samples",
-                      "per_n": {k: round(v, 1) for k, v in acc["numpy"][2].items()}}}
+        "one_core": {"value": res["one"][0], "cores": 1, "per_n": res["one"][1]},
+        "numpy_fft": {"value": res["numpy"][0], "cores": 1, "what": "numpy.fft.fft (pocketfft) on the same samples",
+                      "per_n": res["numpy"][1]}}
 
 
 def run_reference(args, world, rank):
@@ -344,7 +353,9 @@ def run_ours(args, world, rank, local):
                 "kernel": "N=%d %s plan %s" % (dom, "fx" if F.plan_query(dom, eng)["engine"] == F.ENGINE_FX else "f64",
                                                _plan_str(F.plan_query(dom, eng))),
                 "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured" else "fallback 6800 GB/s",
-                "algorithmic_bytes_per_launch": 32 * dom * bufs[dom][2]}
+                "algorithmic_bytes_per_launch": 32 * dom * bufs[dom][2],
+                "per_n": {str(n): {"achieved": per_n[str(n)]["hbm_gbs"], "frac": per_n[str(n)]["frac_hbm"]}
+                          for n in sizes}}
 
     # correctness guard on the timed outputs: 64 transforms per size vs the oracle
     max_err = 0.0
@@ -387,6 +398,8 @@ def run_ours(args, world, rank, local):
         forms["serve"] = bench_serve(args, torch, F)
     if "onchip" in args.forms.split(",") and rank == 0:
         forms["onchip"] = bench_onchip(args, torch, F)
+    if "config1" in args.forms.split(","):
+        forms["config1"] = bench_config1(args, torch, F, dev, stream, world)
     if "cufft" in args.forms.split(","):
         forms["cufft"] = bench_cufft(args, torch, sizes, bufs, stream, per_n)
 
@@ -394,8 +407,9 @@ def run_ours(args, world, rank, local):
     if rank == 0 and not args.no_cpu:
         v, cores, per, extra = cpu_sample_rate(sizes, args.cpu_seconds)
         cpu = {"value": v, "unit": "FFT/s", "cores": cores, "kind": "port",
-               "sample": "oracle FP64 Stockham (radix-8/4/2) on 1/64 of each size's batch, >= %.1f s per size"
-                         % args.cpu_seconds, "per_n": {k: round(val, 1) for k, val in per.items()}}
+               "sample": "oracle FP64 Stockham (radix-8/4/2) on 1/64 of each size's 1 GiB batch, every size once "
+                         "per round (the weighting of value), rounds for >= %.1f s" % args.cpu_seconds,
+               "per_n": per}
         cpu.update(extra)
 
     if rank == 0:
@@ -477,6 +491,61 @@ def bench_split(args, torch, F, dev, stream, world, per_n):
             row[name]["speedup_vs_f64_engine"] = round(row["f64"]["ms"] / row[name]["ms"], 3)
         out["per_n"][str(n)] = row
         del x, y
+    return out
+
+
+def bench_config1(args, torch, F, dev, stream, world):
+    """The small plain configuration: N = 64, batch 65,536 (64 MiB of
+    complex128 in, L2-sized), re/im uniform [-1, 1) from seed 0, through the
+    per-size entry point.  Cold: a 512 MiB write flushes L2 before each
+    launch, and only the launch is timed (CUDA events around it).  Warm:
+    launches back to back on L2-resident buffers.  The reference times its
+    own driver with and without transfers (src/gpu_fft.cu:33-69)."""
+    from fft_onchip_gb300 import inputs
+    from oracle import oracle as O
+    L = F.load()
+    hbm, _ = peaks()
+    n, batch = 64, 65536
+    xh = inputs.uniform(n, batch, seed=0)
+    x = torch.from_numpy(xh).to(dev)
+    y = torch.empty_like(x)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    sptr = stream.cuda_stream
+    K = max(10, args.steps)
+
+    def launch():
+        F.check(L.fftoc_c2c_fwd_n64(x.data_ptr(), y.data_ptr(), batch, sptr))
+
+    for _ in range(3):
+        launch()
+    cold = []
+    for r in range(K):
+        flush.fill_(r & 0xFF)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        launch()
+        b.record(stream)
+        torch.cuda.synchronize()
+        cold.append(a.elapsed_time(b))
+    for _ in range(3):
+        launch()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(K):
+        launch()
+    b.record(stream)
+    torch.cuda.synchronize()
+    warm = a.elapsed_time(b) / K
+    idx = np.arange(0, batch, batch // 64)
+    err = O.rel_l2(y.cpu().numpy()[idx], O.fft_f64(xh[idx]))
+    out = {"workload": "N=64, batch 65536 (64 MiB in), uniform[-1,1) seed 0, fftoc_c2c_fwd_n64",
+           "rel_l2_vs_oracle_64_samples": err}
+    for name, ms in (("cold_l2_flushed", allreduce_max(float(np.median(cold)), world)),
+                     ("warm_back_to_back", allreduce_max(warm, world))):
+        gbs = 32.0 * n * batch / (ms * 1e-3) / 1e9
+        out[name] = {"ms": round(ms, 5), "fft_per_s": world * batch / (ms * 1e-3), "hbm_gbs": round(gbs, 1),
+                     "frac_hbm": round(gbs / hbm, 4)}
+    del x, y, flush
     return out
 
 

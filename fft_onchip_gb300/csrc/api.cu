@@ -98,6 +98,7 @@ struct DeviceState {
   void* tw[2][kNumSizes][kMaxVariants] = {};      // per-variant twiddle tables
   int* err = nullptr;                             // device error flag (bounded waits that gave up)
   int sms = 0;
+  std::atomic<bool> ready{false};                 // set-up done and successful
 };
 
 // Plan chosen per (engine, size): process-wide, set by fftoc_plan_select or
@@ -200,7 +201,10 @@ fftoc_status device_state(DeviceState** out) {
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   if (dev < 0 || dev >= kMaxDevices) return fail(FFTOC_ERR_INVALID_VALUE, "device ordinal out of range");
   DeviceState& ds = g_devices[dev];
-  std::call_once(ds.once, [&] { init_device(ds); });
+  std::call_once(ds.once, [&] {
+    init_device(ds);
+    if (ds.init_status == FFTOC_OK) ds.ready.store(true, std::memory_order_release);
+  });
   if (ds.init_status != FFTOC_OK) return fail(ds.init_status, ds.init_error);
   *out = &ds;
   return FFTOC_OK;
@@ -373,19 +377,33 @@ fftoc_status plan_query(int n, int engine, int variant, fftoc_plan_info* info) {
   return FFTOC_OK;
 }
 
+// Reads and clears the current device's error flags without allocating:
+// the allocation-free entry point's flag (if that path was set up on this
+// device) and the other paths' flag (if their device state exists; checking
+// does not create it, since nothing could have raised a flag that does not
+// exist).
 fftoc_status device_error_check() {
-  DeviceState* ds = nullptr;
-  fftoc_status st = device_state(&ds);
-  if (st != FFTOC_OK) return st;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail(FFTOC_ERR_INVALID_VALUE, "device ordinal out of range");
   int h = 0;
-  cudaError_t e = cudaMemcpy(&h, ds->err, sizeof(int), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(error flag)");
-  if (h != 0) {
-    e = cudaMemset(ds->err, 0, sizeof(int));
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(error flag)");
-    if (h & kErrTimeout) return fail(FFTOC_ERR_TIMEOUT, "a kernel's bounded wait for its prefetched tile gave up");
-    return fail(FFTOC_ERR_INVALID_VALUE, "an uneven batch skipped entries with an unsupported size or a negative offset");
+  fftoc_status st = noalloc_take_error(dev, &h);
+  if (st != FFTOC_OK) return st;
+  DeviceState& ds = g_devices[dev];
+  if (ds.ready.load(std::memory_order_acquire)) {
+    int d = 0;
+    e = cudaMemcpy(&d, ds.err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(error flag)");
+    if (d != 0) {
+      e = cudaMemset(ds.err, 0, sizeof(int));
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(error flag)");
+    }
+    h |= d;
   }
+  if (h & kErrTimeout) return fail(FFTOC_ERR_TIMEOUT, "a kernel's bounded wait for its prefetched tile gave up");
+  if (h != 0)
+    return fail(FFTOC_ERR_INVALID_VALUE, "an uneven batch skipped entries with an unsupported size or a negative offset");
   return FFTOC_OK;
 }
 

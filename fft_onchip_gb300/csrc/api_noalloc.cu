@@ -37,11 +37,13 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 __device__ __align__(256) int4 g_noalloc_twiddles[kNoAllocTwiddleEntries];
 __device__ int g_noalloc_err;
 
-// Per-device set-up, done once by the first call on a device with that device
-// current: addresses of the arrays (a host-side name of a __device__ array is
-// not a device address), twiddle upload, kernel attributes.  No allocation.
+// Per-device set-up, done by the first successful call on a device with that
+// device current: addresses of the arrays (a host-side name of a __device__
+// array is not a device address), twiddle upload, kernel attributes.  No
+// allocation.  A set-up that fails is retried by the next call.
 struct NoAllocDevice {
-  std::once_flag once;
+  std::mutex mu;
+  std::atomic<bool> ready{false};
   fftoc_status status = FFTOC_OK;
   std::string error;
   unsigned char* scratch = nullptr;
@@ -113,6 +115,20 @@ void setup(NoAllocDevice& nd, int dev) {
 
 }  // namespace
 
+fftoc_status noalloc_take_error(int dev, int* flags) {
+  *flags = 0;
+  if (dev < 0 || dev >= kMaxDevices) return FFTOC_OK;
+  NoAllocDevice& nd = g_dev[dev];
+  if (!nd.ready.load(std::memory_order_acquire)) return FFTOC_OK;
+  int h = 0;
+  cudaError_t e = cudaMemcpy(&h, nd.err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return set_error(FFTOC_ERR_CUDA, std::string("cudaMemcpy(error flag): ") + cudaGetErrorString(e));
+  if (h != 0 && (e = cudaMemset(nd.err, 0, sizeof(int))) != cudaSuccess)
+    return set_error(FFTOC_ERR_CUDA, std::string("cudaMemset(error flag): ") + cudaGetErrorString(e));
+  *flags = h;
+  return FFTOC_OK;
+}
+
 fftoc_status launch_fwd_host_noalloc(int n, const double* h_in, double* h_out, int64_t batch, int engine,
                                      cudaStream_t stream) {
   const int idx = size_index(n);
@@ -142,8 +158,16 @@ fftoc_status launch_fwd_host_noalloc(int n, const double* h_in, double* h_out, i
   if (e != cudaSuccess) return set_error(FFTOC_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return set_error(FFTOC_ERR_INVALID_VALUE, "device ordinal out of range");
   NoAllocDevice& nd = g_dev[dev];
-  std::call_once(nd.once, [&] { setup(nd, dev); });
-  if (nd.status != FFTOC_OK) return set_error(nd.status, nd.error);
+  if (!nd.ready.load(std::memory_order_acquire)) {
+    std::lock_guard<std::mutex> lock(nd.mu);
+    if (!nd.ready.load(std::memory_order_relaxed)) {
+      nd.status = FFTOC_OK;
+      nd.error.clear();
+      setup(nd, dev);
+      if (nd.status != FFTOC_OK) return set_error(nd.status, nd.error);
+      nd.ready.store(true, std::memory_order_release);
+    }
+  }
 
   const int slot = eng == FFTOC_ENGINE_FX ? 1 : 0;
   const int var = chosen_variant(slot, idx);

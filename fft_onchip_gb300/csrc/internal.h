@@ -138,6 +138,10 @@ int resolved_engine(int n, int engine);
 // error flag and SM count (device set-up on first use).
 fftoc_status device_plan_resources(int slot, int idx, int var, const void** tw, int** err, int* sms);
 fftoc_status set_error(fftoc_status st, const std::string& msg);
+// api_noalloc.cu: read (into *flags) and clear the allocation-free entry
+// point's device error flag of device `dev`; *flags = 0 if that path has not
+// been set up there.  Allocates nothing.
+fftoc_status noalloc_take_error(int dev, int* flags);
 // Plan variant the uneven-batch path uses for (engine slot, size index), or -1.
 int uneven_variant(int slot, int idx);
 

@@ -147,7 +147,10 @@ fftoc_status fftoc_c2c_fwd_host(int n, const double *h_in, double *h_out, int64_
  * array: calls that overlap on the GPU (other streams, other host threads)
  * race and corrupt each other's results — serialise them.  The first call on
  * a device does the set-up (array addresses, twiddle upload into another
- * compiled-in array, kernel attributes): make it before any stream capture. */
+ * compiled-in array, kernel attributes): make it before any stream capture;
+ * a set-up that fails returns its error and is tried again by the next call.
+ * Device-side failures of this path (a bounded wait that gave up) are
+ * reported by fftoc_device_error_check(), which allocates nothing. */
 fftoc_status fftoc_c2c_fwd_host_noalloc(int n, const double *h_in, double *h_out, int64_t batch, int engine,
                                         fftoc_stream stream);
 
@@ -341,11 +344,13 @@ fftoc_status fftoc_onchip_run(int n, int engine, double *data, int64_t blocks, i
  * resolves to the latter).  Synchronous on first use of a plan. */
 fftoc_status fftoc_exec_twiddles(int n, int engine, const int radix[4], const void **table);
 
-/* Device-side error flag of the current device: FFTOC_ERR_TIMEOUT if a
- * persistent kernel's bounded wait for a prefetched tile gave up since the
- * last check (its outputs are then incomplete), FFTOC_ERR_INVALID_VALUE if an
- * uneven batch skipped entries (bad size or negative offset), FFTOC_OK
- * otherwise.  Clears the flag.  Synchronous. */
+/* Device-side error flags of the current device, those of every entry point
+ * including fftoc_c2c_fwd_host_noalloc: FFTOC_ERR_TIMEOUT if a persistent
+ * kernel's bounded wait for a prefetched tile gave up since the last check
+ * (its outputs are then incomplete), FFTOC_ERR_INVALID_VALUE if an uneven
+ * batch skipped entries (bad size or negative offset), FFTOC_OK otherwise.
+ * Clears the flags.  Synchronous; allocates nothing (and creates no device
+ * state of the library). */
 fftoc_status fftoc_device_error_check(void);
 
 /* Self-test of the failure path of the bounded device waits: one CTA waits

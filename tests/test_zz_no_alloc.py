@@ -3,8 +3,11 @@ allocates no device memory (for callers whose device memory belongs to
 another allocator or a fixed pool, or that cannot take cudaMalloc's implicit
 synchronisation).  Its output must match the allocating host-buffer entry
 point, fftoc_c2c_fwd_host, on two calls in a row (the compiled-in staging
-array is reused and keeps the previous call's contents).  Collected last so a
-failure here cannot hide the rest of the suite; it also passes alone."""
+array is reused and keeps the previous call's contents), match the oracle on
+a strided sample of rows, and leave the device error flags clear (read with
+fftoc_device_error_check, which allocates nothing either).  Pinned and
+pageable host buffers are both accepted.  Collected last so a failure here
+cannot hide the rest of the suite; it also passes alone."""
 import ctypes
 
 import numpy as np
@@ -22,7 +25,7 @@ def _call(L, fn, n, x, out, engine, stream):
     return getattr(L, fn)(n, x.data_ptr(), out.data_ptr(), x.shape[0], engine, stream)
 
 
-@pytest.mark.parametrize("n,engine", [(64, 0), (512, 2), (4096, 0), (256, 1)])
+@pytest.mark.parametrize("n,engine", [(64, 0), (512, 2), (4096, 0), (256, 1), (8, 0)])
 def test_noalloc_matches_allocating_host_path(cuda, fftoc_lib, n, engine):
     torch = cuda
     L = fftoc_lib
@@ -36,9 +39,23 @@ def test_noalloc_matches_allocating_host_path(cuda, fftoc_lib, n, engine):
             L.fftoc_last_error_string()
         assert _call(L, "fftoc_c2c_fwd_host", n, x, ref, engine, s.cuda_stream) == 0
         s.synchronize()
+        assert L.fftoc_device_error_check() == 0, L.fftoc_last_error_string()
         assert O.rel_l2(got.numpy(), ref.numpy()) < TOL, (n, engine, call)
-        k = np.r_[0:4, batch - 4:batch]
+        k = np.r_[np.arange(0, batch, max(1, batch // 64)), batch - 1]
         assert O.rel_l2(got.numpy()[k], O.fft_f64(x.numpy()[k])) < TOL
+
+
+def test_noalloc_pageable_buffers(cuda, fftoc_lib):
+    torch = cuda
+    L = fftoc_lib
+    n, batch = 128, 3000
+    s = torch.cuda.current_stream()
+    x = torch.from_numpy(inputs.uniform(n, batch, seed=9))          # pageable host memory
+    got = torch.full_like(x, float("nan"))
+    assert _call(L, "fftoc_c2c_fwd_host_noalloc", n, x, got, 0, s.cuda_stream) == 0, L.fftoc_last_error_string()
+    s.synchronize()
+    assert L.fftoc_device_error_check() == 0
+    assert O.rel_l2(got.numpy(), O.fft_f64(x.numpy())) < TOL
 
 
 def test_noalloc_rejects_batches_beyond_its_scratch(cuda, fftoc_lib):
