@@ -8,10 +8,12 @@
 //     range of the pool holds it (pool.h);
 //   - packs admitted requests of one engine (the oldest pending request's;
 //     requests of other engines keep their place) into a device batch (up to
-//     max_batch_bytes) and runs it on one of `slots` streams: H2D copy of each
-//     request into its pool range, the batch's offset table, one uneven-batch
-//     graph (fftoc_uneven_execute) over all its transforms, D2H copy of each
-//     request, and a host callback that timestamps completion;
+//     max_batch_bytes; the decision is batching.h's) and runs it on one of
+//     `slots` streams: H2D copy of each request into the pool, then the
+//     plain form's one uneven-batch graph (fftoc_uneven_execute) over all the
+//     batch's transforms, or the split form's one launch per size group (the
+//     requests of one size placed back to back), D2H copy of each request,
+//     and a host callback that timestamps completion;
 //   - keeps forming and launching batches while others are on the GPU, as
 //     stream slots and pool memory free up (continuous batching).
 // Every transform's arithmetic depends only on its own points and its size's
@@ -26,9 +28,12 @@
 #include <unordered_map>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/fftoc.h"
 #include "internal.h"
 #include "pool.h"
+#include "batching.h"
 
 namespace fftoc {
 namespace {
@@ -47,7 +52,8 @@ struct Request {
   const double* h_in = nullptr;
   double* h_out = nullptr;
   int64_t bytes = 0;
-  int64_t pool_off = -1;
+  int64_t pool_off = -1;   // where the request's data sit in the pool
+  int64_t range_off = -1;  // the pool range it releases (-1: none; a split size group's other requests)
   double submit_us = 0, launch_us = 0, done_us = 0;
   int state = 0;  // 0 pending, 1 in flight, 2 done
   fftoc_status status = FFTOC_OK;
@@ -81,6 +87,7 @@ struct fftoc_server_s {
   std::condition_variable cv_done;  // request completion
   std::deque<int64_t> pending;
   std::unordered_map<int64_t, fftoc::Request> reqs;
+  std::unordered_map<int64_t, fftoc::SchedReq> sreqs;  // pending requests, as the batching decision sees them
   std::vector<int> completed_slots;
   int64_t next_id = 1;
   bool stop = false;
@@ -120,52 +127,41 @@ void CUDART_CB batch_done(void* p) {
 
 // Enqueue one batch on its slot (scheduler thread, lock NOT held).  Plain
 // form: one uneven-batch graph over all the batch's transforms.  Split form:
-// each request is contiguous in the pool, one launch per request.
-fftoc_status enqueue_batch(fftoc_server_s* s, int si, const std::vector<Request*>& rs, int engine,
-                           int64_t transforms) {
+// one launch per size group (its requests back to back in one pool range).
+fftoc_status enqueue_batch(fftoc_server_s* s, int si, const Batch& b, const std::vector<Request*>& rs) {
   Slot& sl = s->slots[si];
   cudaError_t e;
-  if (is_split_engine(engine)) {
-    for (const Request* r : rs) {
-      if ((e = cudaMemcpyAsync(s->pool_base + r->pool_off, r->h_in, (size_t)r->bytes, cudaMemcpyHostToDevice,
-                               sl.stream)) != cudaSuccess)
-        return cuda_fail(e, "cudaMemcpyAsync(request in)");
-      double* buf = reinterpret_cast<double*>(s->pool_base + r->pool_off);
-      const fftoc_status st = launch_split(r->n, buf, buf, r->count, split_kind_of(engine), sl.stream);
-      if (st != FFTOC_OK) return st;
-      if ((e = cudaMemcpyAsync(r->h_out, s->pool_base + r->pool_off, (size_t)r->bytes, cudaMemcpyDeviceToHost,
-                               sl.stream)) != cudaSuccess)
-        return cuda_fail(e, "cudaMemcpyAsync(request out)");
-    }
-    CallbackData* cd = new CallbackData{s, si};
-    if ((e = cudaLaunchHostFunc(sl.stream, batch_done, cd)) != cudaSuccess) {
-      delete cd;
-      return cuda_fail(e, "cudaLaunchHostFunc");
-    }
-    return FFTOC_OK;
-  }
-  const int engine_slot = engine == FFTOC_ENGINE_F64 ? 0 : 1;
-  int64_t k = 0;
-  for (const Request* r : rs) {
-    const int64_t base = r->pool_off / 16;  // complex elements from the pool base
-    for (int64_t t = 0; t < r->count; ++t, ++k) {
-      sl.h_off[k] = base + t * r->n;
-      sl.h_ns[k] = r->n;
-    }
-  }
-  double* pool = reinterpret_cast<double*>(s->pool_base);
   for (const Request* r : rs)
     if ((e = cudaMemcpyAsync(s->pool_base + r->pool_off, r->h_in, (size_t)r->bytes, cudaMemcpyHostToDevice,
                              sl.stream)) != cudaSuccess)
       return cuda_fail(e, "cudaMemcpyAsync(request in)");
-  if ((e = cudaMemcpyAsync(sl.d_off, sl.h_off, (size_t)transforms * 8, cudaMemcpyHostToDevice, sl.stream)) !=
-      cudaSuccess)
-    return cuda_fail(e, "cudaMemcpyAsync(offsets)");
-  if ((e = cudaMemcpyAsync(sl.d_ns, sl.h_ns, (size_t)transforms * 4, cudaMemcpyHostToDevice, sl.stream)) != cudaSuccess)
-    return cuda_fail(e, "cudaMemcpyAsync(sizes)");
-  fftoc_status st = fftoc_uneven_execute(sl.plan[engine_slot], pool, pool, sl.d_off, sl.d_ns, transforms,
-                                         (fftoc_stream)sl.stream);
-  if (st != FFTOC_OK) return st;
+  if (is_split_engine(b.engine)) {
+    for (const SizeGroup& g : b.groups) {
+      double* buf = reinterpret_cast<double*>(s->pool_base + g.pool_off);
+      const fftoc_status st = launch_split(g.n, buf, buf, g.count, split_kind_of(b.engine), sl.stream);
+      if (st != FFTOC_OK) return st;
+    }
+  } else {
+    const int engine_slot = b.engine == FFTOC_ENGINE_F64 ? 0 : 1;
+    int64_t k = 0;
+    for (const Request* r : rs) {
+      const int64_t base = r->pool_off / 16;  // complex elements from the pool base
+      for (int64_t t = 0; t < r->count; ++t, ++k) {
+        sl.h_off[k] = base + t * r->n;
+        sl.h_ns[k] = r->n;
+      }
+    }
+    double* pool = reinterpret_cast<double*>(s->pool_base);
+    if ((e = cudaMemcpyAsync(sl.d_off, sl.h_off, (size_t)b.transforms * 8, cudaMemcpyHostToDevice, sl.stream)) !=
+        cudaSuccess)
+      return cuda_fail(e, "cudaMemcpyAsync(offsets)");
+    if ((e = cudaMemcpyAsync(sl.d_ns, sl.h_ns, (size_t)b.transforms * 4, cudaMemcpyHostToDevice, sl.stream)) !=
+        cudaSuccess)
+      return cuda_fail(e, "cudaMemcpyAsync(sizes)");
+    const fftoc_status st = fftoc_uneven_execute(sl.plan[engine_slot], pool, pool, sl.d_off, sl.d_ns, b.transforms,
+                                                 (fftoc_stream)sl.stream);
+    if (st != FFTOC_OK) return st;
+  }
   for (const Request* r : rs)
     if ((e = cudaMemcpyAsync(r->h_out, s->pool_base + r->pool_off, (size_t)r->bytes, cudaMemcpyDeviceToHost,
                              sl.stream)) != cudaSuccess)
@@ -184,8 +180,8 @@ void retire(fftoc_server_s* s, int si) {  // lock held
     auto it = s->reqs.find(id);
     if (it == s->reqs.end()) continue;
     Request& r = it->second;
-    s->pool->release(r.pool_off);
-    r.pool_off = -1;
+    if (r.range_off >= 0) s->pool->release(r.range_off);
+    r.pool_off = r.range_off = -1;
     r.done_us = sl.done_us;
     r.state = 2;
     s->requests_done += 1;
@@ -199,8 +195,8 @@ void retire(fftoc_server_s* s, int si) {  // lock held
 
 void fail_requests(fftoc_server_s* s, const std::vector<Request*>& rs, fftoc_status st) {  // lock held
   for (Request* r : rs) {
-    if (r->pool_off >= 0) s->pool->release(r->pool_off);
-    r->pool_off = -1;
+    if (r->range_off >= 0) s->pool->release(r->range_off);
+    r->pool_off = r->range_off = -1;
     r->state = 2;
     r->status = st;
     r->done_us = now_us(s->t0);
@@ -217,7 +213,10 @@ void scheduler(fftoc_server_s* s) {
     if (s->stop) {
       // shutting down: requests not yet on the GPU fail, batches in flight finish
       std::vector<Request*> left;
-      for (int64_t id : s->pending) left.push_back(&s->reqs[id]);
+      for (int64_t id : s->pending) {
+        left.push_back(&s->reqs[id]);
+        s->sreqs.erase(id);
+      }
       s->pending.clear();
       fail_requests(s, left, FFTOC_ERR_INVALID_VALUE);
       bool any = false;
@@ -227,50 +226,31 @@ void scheduler(fftoc_server_s* s) {
       continue;
     }
     bool waiting_window = false;
+    const SchedConfig cfg{s->cfg.max_batch_bytes, s->cfg.max_wait_us, s->max_count};
+    auto lookup = [s](int64_t id) -> const SchedReq& { return s->sreqs[id]; };
     while (!s->stop && !s->pending.empty()) {
       int si = -1, inflight = 0;
       for (int i = 0; i < (int)s->slots.size(); ++i) {
         if (s->slots[i].busy) ++inflight;
         else if (si < 0) si = i;
       }
-      if (si < 0) break;  // all slots busy: wait for a completion
-      // launch when the batch is full, the oldest request has waited the
-      // batching window, or the GPU has nothing in flight
-      const Request& head = s->reqs[s->pending.front()];
-      int64_t queued = 0;
-      for (int64_t id : s->pending) {
-        queued += s->reqs[id].bytes;
-        if (queued >= s->cfg.max_batch_bytes) break;
-      }
       const double now = now_us(s->t0);
-      if (inflight > 0 && queued < s->cfg.max_batch_bytes && now - head.submit_us < s->cfg.max_wait_us) {
-        waiting_window = true;
-        break;
-      }
-      // admit in arrival order the requests of the oldest request's engine
-      // (others keep their place), batch bytes and transforms within limits,
-      // each into a free pool range; stop at the first that does not fit
-      const int engine = head.engine;
+      Batch b;
+      nvtxRangePushA("fftoc.serve.form_batch");
+      const SchedStep step = form_batch(s->pending, lookup, is_split_engine, si >= 0, inflight, now, cfg, *s->pool, &b);
+      nvtxRangePop();
+      if (step == SchedStep::kWaitWindow) waiting_window = true;
+      if (step != SchedStep::kLaunch) break;
       std::vector<Request*> batch;
-      int64_t bytes = 0, transforms = 0;
-      for (auto it = s->pending.begin(); it != s->pending.end();) {
-        Request& r = s->reqs[*it];
-        if (r.engine != engine) {
-          ++it;
-          continue;
-        }
-        if (!batch.empty() && (bytes + r.bytes > s->cfg.max_batch_bytes || transforms + r.count > s->max_count)) break;
-        const int64_t off = s->pool->alloc(r.bytes);
-        if (off < 0) break;  // wait for memory to free up
-        r.pool_off = off;
+      for (const Placement& p : b.reqs) {
+        Request& r = s->reqs[p.id];
+        r.pool_off = p.pool_off;
+        r.range_off = p.range_off;
         r.state = 1;
         r.launch_us = now;
-        bytes += r.bytes;
-        transforms += r.count;
+        s->sreqs.erase(p.id);
         batch.push_back(&r);
-        it = s->pending.erase(it);
       }
-      if (batch.empty()) break;
       Slot& sl = s->slots[si];
       sl.busy = true;
       sl.reqs.clear();
@@ -278,7 +258,9 @@ void scheduler(fftoc_server_s* s) {
       s->batches += 1;
       if (inflight + 1 > s->max_inflight) s->max_inflight = inflight + 1;
       lk.unlock();
-      const fftoc_status st = enqueue_batch(s, si, batch, engine, transforms);
+      nvtxRangePushA(is_split_engine(b.engine) ? "fftoc.serve.enqueue_split" : "fftoc.serve.enqueue_plain");
+      const fftoc_status st = enqueue_batch(s, si, b, batch);
+      nvtxRangePop();
       lk.lock();
       if (st != FFTOC_OK) {
         // the stream may hold part of the batch: drain it before reusing the ranges
@@ -404,6 +386,14 @@ fftoc_status submit(fftoc_server_s* s, int n, int64_t count, int engine, const d
     r.id = s->next_id++;
     r.submit_us = now_us(s->t0);
     s->reqs[r.id] = r;
+    fftoc::SchedReq q;
+    q.id = r.id;
+    q.n = r.n;
+    q.count = r.count;
+    q.engine = r.engine;
+    q.bytes = r.bytes;
+    q.submit_us = r.submit_us;
+    s->sreqs[r.id] = q;
     s->pending.push_back(r.id);
     *id = r.id;
   }

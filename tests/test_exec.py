@@ -80,6 +80,41 @@ def test_executor_shape_contract(harness, n, engine):
     assert harness.exec_harness_shape(n + 1, ENGINES[engine], *[ctypes.byref(ctypes.c_int()) for _ in range(4)]) == -2
 
 
+def test_compat_names_take_the_reference_parameter_lists(tmp_path):
+    """include/fftoc/compat.cuh: the reference's executor names with their
+    template parameter lists and defaults (includes/tensor_fft_64.cuh:12,
+    tensor_fft_4096.cuh:12, tensor_fft_8.cuh:12, legacy8_fft.cuh:11,
+    legacy16_fft.cuh:17) name this library's executors."""
+    from fft_onchip_gb300 import build
+    src = tmp_path / "compat_check.cu"
+    src.write_text(r"""
+#include <type_traits>
+#include <thrust/complex.h>
+#include <fftoc/compat.cuh>
+namespace fft = fftoc::compat;
+using CT = thrust::complex<double>;
+static_assert(std::is_same<fft::tensor_fft_64<CT, 64>, fftoc::exec::fft<CT, 64, 2>>::value, "");
+static_assert(std::is_same<fft::tensor_fft_64<CT, 64, 4, 1>, fftoc::exec::fft<CT, 64, 4>>::value, "");
+static_assert(std::is_same<fft::tensor_fft_8<CT, 8>, fftoc::exec::fft<CT, 8, 1>>::value, "");
+static_assert(std::is_same<fft::tensor_fft_4096<CT, 4096>, fftoc::exec::fft<CT, 4096, 1>>::value, "");
+static_assert(std::is_same<fft::legacy_fft<CT, 512>, fftoc::exec::fft<CT, 512, 1>>::value, "");
+static_assert(std::is_same<fft::legacy16_fft<CT, 256>, fftoc::exec::fft<CT, 256, 1>>::value, "");
+static_assert(fft::tensor_fft_256<CT, 256, 2, 1>::units_per_block == 2, "");
+template <class Exec>
+__global__ void __launch_bounds__(Exec::max_threads_per_block) run(CT* d) {
+  extern __shared__ __align__(16) char sh[];
+  Exec f(reinterpret_cast<CT*>(sh));
+  f();
+}
+template __global__ void run<fft::tensor_fft_64<CT, 64>>(CT*);
+template __global__ void run<fft::legacy_fft<CT, 512>>(CT*);
+""")
+    r = subprocess.run([build.nvcc()] + build.ARCH + ["-std=c++17", "-I" + os.path.join(ROOT, "include"), "-c",
+                                                      str(src), "-o", str(tmp_path / "compat_check.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+
+
 def test_exec_twiddles_argument_errors(fftoc_lib):
     L = fftoc_lib
     out = ctypes.c_void_p(1)

@@ -1,6 +1,7 @@
 """CPU tests of the serving loop's host parts: the pool's range allocator
-(tests/host/pool_check.cpp against a unit-by-unit model) and the request
-trace generator."""
+(tests/host/pool_check.cpp against a unit-by-unit model), the batching
+decision driven by a CPU executor on a simulated clock
+(tests/host/sched_check.cpp), and the request trace generator."""
 import os
 import shutil
 import subprocess
@@ -21,6 +22,22 @@ def test_pool_allocator_against_model():
     subprocess.run([gxx, "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "fft_onchip_gb300", "csrc"),
                     "-o", exe, os.path.join(ROOT, "tests", "host", "pool_check.cpp")], check=True)
     r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.startswith("ok"), r.stdout
+
+
+def test_batching_decision_with_cpu_executor():
+    """Admission order, batch limits, the batching window, split-form size
+    groups and pool accounting of fft_onchip_gb300/csrc/batching.h, with a CPU
+    stand-in for the device that moves and transforms each request's data."""
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ not available")
+    out_dir = os.path.join(ROOT, "tests", "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    exe = os.path.join(out_dir, "sched_check")
+    subprocess.run([gxx, "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "fft_onchip_gb300", "csrc"),
+                    "-o", exe, os.path.join(ROOT, "tests", "host", "sched_check.cpp")], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and r.stdout.startswith("ok"), r.stdout
 
 
