@@ -266,7 +266,10 @@ fftoc_status launch_fwd(int n, const double* in, double* out, int64_t batch, int
   if (a != b && a < b + bytes && b < a + bytes) return fail(FFTOC_ERR_INVALID_VALUE, "in and out overlap partially");
 
   const int eng = resolve_engine(n, engine);
-  if (eng == FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_UNSUPPORTED, "DMMA engine not available for n=" + std::to_string(n));
+  if (eng == FFTOC_ENGINE_DMMA) {
+    if (variant > 0) return fail(FFTOC_ERR_INVALID_VALUE, "no such plan variant");
+    return launch_dmma(n, in, out, batch, stream);
+  }
   if (is_split_engine(eng)) return launch_split(n, in, out, batch, split_kind_of(eng), stream);
   DeviceState* ds = nullptr;
   fftoc_status st = device_state(&ds);
@@ -346,7 +349,10 @@ fftoc_status plan_query(int n, int engine, int variant, fftoc_plan_info* info) {
   if (!info) return fail(FFTOC_ERR_INVALID_VALUE, "null info");
   if (engine < FFTOC_ENGINE_AUTO || engine > kLastEngine) return fail(FFTOC_ERR_INVALID_VALUE, "unknown engine");
   const int eng = resolve_engine(n, engine);
-  if (eng == FFTOC_ENGINE_DMMA) return fail(FFTOC_ERR_UNSUPPORTED, "DMMA engine not available for n=" + std::to_string(n));
+  if (eng == FFTOC_ENGINE_DMMA) {
+    if (variant > 0) return fail(FFTOC_ERR_INVALID_VALUE, "no such plan variant");
+    return dmma_plan_info(n, info);
+  }
   if (is_split_engine(eng)) {
     if (variant > 0) return fail(FFTOC_ERR_INVALID_VALUE, "no such plan variant");
     const fftoc_status st = split_plan_info(n, split_kind_of(eng), info);
@@ -412,7 +418,9 @@ fftoc_status plan_select(int n, int engine, int variant) {
   fftoc_status st = plan_query(n, engine, variant < 0 ? 0 : variant, &info);
   if (st != FFTOC_OK) return st;
   if (variant < 0) return fail(FFTOC_ERR_INVALID_VALUE, "variant must be >= 0");
-  g_choice[info.engine == FFTOC_ENGINE_FX ? 1 : 0][size_index(n)].store(variant);
+  // engines with one plan per size (split forms, DMMA) have no choice to store
+  if (info.engine == FFTOC_ENGINE_FX || info.engine == FFTOC_ENGINE_F64)
+    g_choice[info.engine == FFTOC_ENGINE_FX ? 1 : 0][size_index(n)].store(variant);
   return FFTOC_OK;
 }
 
@@ -463,7 +471,8 @@ fftoc_status autotune(int n, int engine, int64_t batch, cudaStream_t stream, int
   cudaFree(y);
   if (st != FFTOC_OK) return st;
   if (e != cudaSuccess) return cuda_fail(e, "autotune");
-  g_choice[info.engine == FFTOC_ENGINE_FX ? 1 : 0][size_index(n)].store(bestv);
+  if (info.engine == FFTOC_ENGINE_FX || info.engine == FFTOC_ENGINE_F64)
+    g_choice[info.engine == FFTOC_ENGINE_FX ? 1 : 0][size_index(n)].store(bestv);
   if (best_variant) *best_variant = bestv;
   if (best_ms) *best_ms = best;
   return FFTOC_OK;

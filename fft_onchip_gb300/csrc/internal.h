@@ -126,6 +126,11 @@ inline cudaError_t fit_carveout(const void* fn, int threads, int smem, int* bloc
 constexpr int kErrTimeout = 1;        // a bounded wait for a prefetched tile gave up
 constexpr int kErrUnevenSkipped = 2;  // uneven-batch entries with a bad size or offset were skipped
 
+// api_dmma.cu: FFTOC_ENGINE_DMMA (n = 8)
+bool dmma_supported(int n);
+fftoc_status dmma_plan_info(int n, fftoc_plan_info* info);
+fftoc_status launch_dmma(int n, const double* in, double* out, int64_t batch, cudaStream_t stream);
+
 // api.cu accessors: compiled plans per engine slot (0 F64, 1 FX), twiddle
 // tables of a plan (16 bytes per entry: double2 / 4 x int32 limbs), the plan
 // currently chosen for (slot, size index), AUTO resolution, and the

@@ -65,8 +65,11 @@ typedef enum {
   FFTOC_ENGINE_FX = 2,   /* 64-bit block fixed point: per-transform power-of-two
                             scale, exact integer adds, 60-bit twiddles;
                             relative L2 error ~1e-15                             */
-  FFTOC_ENGINE_DMMA = 3, /* Karatsuba complex GEMM on FP64 mma.m8n8k4
-                            (the reference's tensor_utils.cuh:32-36 scheme)      */
+  FFTOC_ENGINE_DMMA = 3, /* IEEE binary64 on the FP64 tensor cores: the
+                            Karatsuba complex product (3 real 8x8x8 products,
+                            the reference's tensor_utils.cuh:25-36 scheme) of
+                            the exact DFT matrix, n = 8 only
+                            (FFTOC_ERR_UNSUPPORTED for other n)                 */
   FFTOC_ENGINE_SPLIT_BF16X3 = 4, /* split-precision form, 3 BF16 terms per
                             operand on the tensor cores, FP32 accumulation and
                             data (relative L2 error ~1e-7; n >= 16)              */
