@@ -163,13 +163,26 @@ struct EngFxT {
     return (S)a * (S)b + c;
 #endif
   }
+  // a*b with a, b 32-bit: one IMAD.WIDE without an addend
+  FFTOC_HD static S mulw(int a, int b) {
+#ifdef __CUDA_ARCH__
+    S d;
+    asm("mul.wide.s32 %0, %1, %2;" : "=l"(d) : "r"(a), "r"(b));
+    return d;
+#else
+    return (S)a * (S)b;
+#endif
+  }
   // x * c for a real constant, |c| <= 1:
   //   x*c = xh*ch + (xh*cl + xl*ch) / 2^30 + xl*cl/2^60   (last term < 1, dropped)
-  // |xh*cl| < 2^61, |xl*ch| <= 2^60, so the middle sum cannot overflow.
+  // |xh*cl| < 2^61, |xl*ch| <= 2^60, so the middle sum cannot overflow.  The
+  // middle sum is shifted without a rounding constant (floor): the product is
+  // within 2 units of the exact value, and a chain that opens with a plain
+  // multiply measured 2-4 % faster than one that opens with a 64-bit addend.
   FFTOC_HD static S mulc(S x, KC k) {
     int xh, xl;
     split(x, xh, xl);
-    const long long m = madw(xl, k.h, madw(xh, k.l, 1LL << 29));
+    const long long m = madw(xl, k.h, mulw(xh, k.l));
     return madw(xh, k.h, m >> 30);
   }
   // (xr + i xi) * (wr + i wi); each middle sum has four terms of magnitude
@@ -181,8 +194,8 @@ struct EngFxT {
     // negate the twiddle limbs (|wih| <= 2^30, 0 <= wil < 2^30), never the
     // data limbs (ih may be -2^31)
     const int nwih = -wih, nwil = -wil;
-    const long long mr = madw(il, nwih, madw(ih, nwil, madw(rl, wrh, madw(rh, wrl, 1LL << 29))));
-    const long long mi = madw(il, wrh, madw(ih, wrl, madw(rl, wih, madw(rh, wil, 1LL << 29))));
+    const long long mr = madw(il, nwih, madw(ih, nwil, madw(rl, wrh, mulw(rh, wrl))));
+    const long long mi = madw(il, wrh, madw(ih, wrl, madw(rl, wih, mulw(rh, wil))));
     xr = madw(ih, nwih, madw(rh, wrh, mr >> 30));
     xi = madw(ih, wrh, madw(rh, wih, mi >> 30));
   }
