@@ -177,44 +177,52 @@ def _timed(fn, x, seconds):
             return reps * x.shape[0], el
 
 
-def cpu_sample_rate(sizes, seconds):
-    """The port on all host threads (the baseline), plus two secondary points
-    on the same samples: the port on one thread and numpy.fft (pocketfft,
-    one thread).  Each size's sample is 1/64 of its 1 GiB batch, and every
-    round runs each sample once, so the per-size weighting is the GPU
-    `value`'s (transforms in proportion to 1 GiB / (16 N)); rounds repeat
-    until the leg has run `seconds` (the 1-thread legs a third of it).
-    Each leg's figure is FFT/s over the sweep (transforms / summed time)."""
-    import numpy as np
+CPU_FRACTION = 32  # CPU samples: 1/32 of each size's 1 GiB batch (the reference arm's and cpu_baseline's)
+
+
+def cpu_samples(sizes):
     from fft_onchip_gb300 import inputs
+    return {n: inputs.normal(n, max(1, (GIB // (16 * n)) // CPU_FRACTION), seed=n) for n in sizes}
+
+
+def cpu_sweep(fn, samples, sizes, seconds):
+    """Rounds of fn over every size's sample (each size once per round, so the
+    per-size weighting is the GPU `value`'s: transforms in proportion to
+    1 GiB / (16 N)) until `seconds` have run; (FFT/s, per-size FFT/s, rounds)."""
+    ffts, el, per, rounds = 0, 0.0, {n: [0, 0.0] for n in sizes}, 0
+    while rounds == 0 or el < seconds:
+        for n in sizes:
+            t0 = time.perf_counter()
+            fn(samples[n])
+            dt = time.perf_counter() - t0
+            ffts += samples[n].shape[0]
+            el += dt
+            per[n][0] += samples[n].shape[0]
+            per[n][1] += dt
+        rounds += 1
+    return ffts / el, {str(n): round(v[0] / v[1], 1) for n, v in per.items()}, rounds
+
+
+def cpu_sample_rate(sizes, seconds):
+    """The port on all host threads (the baseline, measured as the reference
+    arm measures it), plus two secondary points on the same samples: the
+    port on one thread and numpy.fft (pocketfft, one thread), each for a
+    third of the time."""
+    import numpy as np
     from oracle import oracle as O
     threads = O.max_threads()
-    samples = {n: inputs.normal(n, max(1, (GIB // (16 * n)) // 64), seed=n) for n in sizes}
+    samples = cpu_samples(sizes)
     for n in sizes:  # warm the pool and caches
         O.fft_f64(samples[n][: max(1, samples[n].shape[0] // 16)], threads=0)
-    legs = {"all": (lambda x: O.fft_f64(x, threads=0), seconds),
-            "one": (lambda x: O.fft_f64(x, threads=1), seconds / 3),
-            "numpy": (lambda x: np.fft.fft(x, axis=1), seconds / 3)}
-    res = {}
-    for k, (fn, sec) in legs.items():
-        ffts, el, per, rounds = 0, 0.0, {n: [0, 0.0] for n in sizes}, 0
-        while rounds == 0 or el < sec:
-            for n in sizes:
-                t0 = time.perf_counter()
-                fn(samples[n])
-                dt = time.perf_counter() - t0
-                ffts += samples[n].shape[0]
-                el += dt
-                per[n][0] += samples[n].shape[0]
-                per[n][1] += dt
-            rounds += 1
-        res[k] = (ffts / el, {str(n): round(v[0] / v[1], 1) for n, v in per.items()}, rounds)
-    return res["all"][0], threads, res["all"][1], {
-        "rounds": res["all"][2],
+    v_all, per_all, rounds = cpu_sweep(lambda x: O.fft_f64(x, threads=0), samples, sizes, seconds)
+    v_one, per_one, _ = cpu_sweep(lambda x: O.fft_f64(x, threads=1), samples, sizes, seconds / 3)
+    v_np, per_np, _ = cpu_sweep(lambda x: np.fft.fft(x, axis=1), samples, sizes, seconds / 3)
+    return v_all, threads, per_all, {
+        "rounds": rounds,
         "nproc": os.cpu_count(),
-        "one_core": {"value": res["one"][0], "cores": 1, "per_n": res["one"][1]},
-        "numpy_fft": {"value": res["numpy"][0], "cores": 1, "what": "numpy.fft.fft (pocketfft) on the same samples",
-                      "per_n": res["numpy"][1]}}
+        "one_core": {"value": v_one, "cores": 1, "per_n": per_one},
+        "numpy_fft": {"value": v_np, "cores": 1, "what": "numpy.fft.fft (pocketfft) on the same samples",
+                      "per_n": per_np}}
 
 
 def run_reference(args, world, rank):
@@ -222,25 +230,22 @@ def run_reference(args, world, rank):
         return
     sizes = [int(s) for s in args.sizes.split(",")]
     from oracle import oracle as O
-    from fft_onchip_gb300 import inputs
     threads = O.max_threads()
-    samples = {}
-    for n in sizes:
-        batch = GIB // (16 * n)
-        samples[n] = inputs.normal(n, max(1, batch // 32), seed=n)
+    samples = cpu_samples(sizes)
+    fn = lambda x: O.fft_f64(x, threads=0)
     for _ in range(args.warmup):
         for n in sizes:
-            O.fft_f64(samples[n], threads=0)
+            fn(samples[n])
     t0 = time.perf_counter()
     ffts = 0
     for _ in range(args.steps):
         for n in sizes:
-            O.fft_f64(samples[n], threads=0)
+            fn(samples[n])
             ffts += samples[n].shape[0]
     el = time.perf_counter() - t0
     value = ffts / el
-    desc = "1/32 of each size's 1 GiB batch per step (%s transforms)" % (
-        "+".join(str(samples[n].shape[0]) for n in sizes))
+    desc = "1/%d of each size's 1 GiB batch per step (%s transforms)" % (
+        CPU_FRACTION, "+".join(str(samples[n].shape[0]) for n in sizes))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "FFT/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
@@ -407,8 +412,9 @@ def run_ours(args, world, rank, local):
     if rank == 0 and not args.no_cpu:
         v, cores, per, extra = cpu_sample_rate(sizes, args.cpu_seconds)
         cpu = {"value": v, "unit": "FFT/s", "cores": cores, "kind": "port",
-               "sample": "oracle FP64 Stockham (radix-8/4/2) on 1/64 of each size's 1 GiB batch, every size once "
-                         "per round (the weighting of value), rounds for >= %.1f s" % args.cpu_seconds,
+               "sample": "oracle FP64 Stockham (radix-8/4/2) on 1/%d of each size's 1 GiB batch, every size once "
+                         "per round (the weighting of value and of the reference arm), rounds for >= %.1f s"
+                         % (CPU_FRACTION, args.cpu_seconds),
                "per_n": per}
         cpu.update(extra)
 
