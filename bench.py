@@ -348,15 +348,16 @@ def run_ours(args, world, rank, local):
     # taken on the plan that ran here
     tt = traffic_table().get(str(dom), {})
     dom_plan = F.plan_query(dom, eng)
-    traffic = tt.get("fx" if dom_plan["engine"] == F.ENGINE_FX else "f64")
+    ename = {F.ENGINE_FX: "fx", F.ENGINE_F64: "f64", F.ENGINE_DMMA: "dmma", F.ENGINE_SPLIT_BF16X3: "split_bf16x3",
+             F.ENGINE_SPLIT_TF32X2: "split_tf32x2", F.ENGINE_SPLIT_EXACT: "split_exact"}.get(dom_plan["engine"], "?")
+    traffic = tt.get(ename) if ename in ("fx", "f64") else None
     if tt.get("plan") != _plan_str(dom_plan):
         traffic = None
     elif traffic is not None:  # the table holds a 1 GiB launch; scale to this launch's transforms
         traffic = int(round(traffic * bufs[dom][2] / (GIB // (16 * dom))))
     roofline = {"bound": "hbm", "achieved": round(dom_gbs, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(dom_gbs / hbm, 4), "traffic": traffic,
-                "kernel": "N=%d %s plan %s" % (dom, "fx" if F.plan_query(dom, eng)["engine"] == F.ENGINE_FX else "f64",
-                                               _plan_str(F.plan_query(dom, eng))),
+                "kernel": "N=%d %s plan %s" % (dom, ename, _plan_str(dom_plan)),
                 "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured" else "fallback 6800 GB/s",
                 "algorithmic_bytes_per_launch": 32 * dom * bufs[dom][2],
                 "per_n": {str(n): {"achieved": per_n[str(n)]["hbm_gbs"], "frac": per_n[str(n)]["frac_hbm"]}
@@ -422,7 +423,10 @@ def run_ours(args, world, rank, local):
         resolved = sorted({F.plan_query(n, eng)["engine"] for n in sizes})
         names = {F.ENGINE_FX: "int64 block fixed point (complex128 in/out)", F.ENGINE_F64: "f64",
                  F.ENGINE_SPLIT_BF16X3: "bf16x3 split on tensor cores, fp32 accumulation (complex128 in/out)",
-                 F.ENGINE_SPLIT_TF32X2: "tf32x2 split on tensor cores, fp32 accumulation (complex128 in/out)"}
+                 F.ENGINE_SPLIT_TF32X2: "tf32x2 split on tensor cores, fp32 accumulation (complex128 in/out)",
+                 F.ENGINE_DMMA: "f64 (FP64 tensor cores)",
+                 F.ENGINE_SPLIT_EXACT: "int64 block fixed point, 8-bit digit slices exact on bf16 tensor cores "
+                                       "(complex128 in/out)"}
         dtype = names.get(resolved[0], "mixed") if len(resolved) == 1 else "mixed"
         line = {
             "metric": METRIC, "value": value, "unit": "FFT/s", "n_gpus": world, "steps": K,

@@ -8,6 +8,7 @@
 
 #include "../../include/fftoc.h"
 #include "internal.h"
+#include "exact_operand.h"
 
 namespace fftoc {
 namespace {
@@ -89,39 +90,6 @@ std::vector<unsigned char> dft16_operand(int esize, int slices) {
           memcpy(&out[off], &t, 4);
           rest -= (double)u32_f(t);
         }
-      }
-    }
-  return out;
-}
-
-// The same matrix for the exact-slice form: entries scaled by 2^47 (rounded
-// from long double) and cut into six balanced 8-bit digits, most significant
-// first, as BF16.
-std::vector<unsigned char> dft16_exact_operand() {
-  const int row_bytes = 64, kc = 4, per_chunk = 8;
-  std::vector<unsigned char> out((size_t)6 * 32 * row_bytes, 0);
-  const long double pi = 3.141592653589793238462643383279502884L;
-  for (int c = 0; c < 32; ++c)
-    for (int k = 0; k < 32; ++k) {
-      const int cc = c & 15, kk = k & 15;
-      const long double ang = -2.0L * pi * (long double)((cc * kk) % 16) / 16.0L;
-      const long double fr = cosl(ang), fi = sinl(ang);
-      long double v;
-      if (c < 16) v = k < 16 ? fr : -fi;
-      else v = k < 16 ? fi : fr;
-      long long t = llroundl(v * 140737488355328.0L);  // 2^47
-      int dig[6];
-      for (int q = 5; q >= 1; --q) {
-        const int d = (int)(signed char)(t & 0xFF);
-        dig[q] = d;
-        t = (t - d) >> 8;
-      }
-      dig[0] = (int)t;  // |t| <= 128
-      for (int q = 0; q < 6; ++q) {
-        const size_t off = (size_t)q * 32 * row_bytes +
-                           (size_t)(((c >> 3) * kc + k / per_chunk) * 128 + (c & 7) * 16 + (k % per_chunk) * 2);
-        const uint16_t h = bf16_rn((float)dig[q]);  // exact: |digit| <= 128
-        memcpy(&out[off], &h, 2);
       }
     }
   return out;

@@ -106,3 +106,46 @@ def test_fx_out_matches_ldexp_in_the_normal_range(engine_report):
 def test_fx_constants_are_rounded_limbs(engine_report):
     # sqrt(1/2), cos(pi/8), sin(pi/8) and negatives as 30-bit limbs of v*2^60
     assert engine_report["fx_konst_ulp"] <= 0.5
+
+
+@pytest.fixture(scope="module")
+def exact_report():
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    out_dir = os.path.join(ROOT, "tests", "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    exe = os.path.join(out_dir, "exact_check")
+    src = os.path.join(ROOT, "tests", "host", "exact_check.cu")
+    csrc = os.path.join(ROOT, "fft_onchip_gb300", "csrc")
+    subprocess.run([nvcc, "-std=c++17", "--expt-relaxed-constexpr", "-gencode", "arch=compute_103a,code=sm_103a",
+                    "-I" + csrc, "-I" + os.path.join(ROOT, "include"), "-o", exe, src], check=True)
+    r = subprocess.run([exe], check=True, capture_output=True, text=True)
+    return {k: float(v) for k, v in (line.split() for line in r.stdout.strip().splitlines())}
+
+
+def test_exact_digit_cut(exact_report):
+    """The offset-binary byte cut gives balanced digits whose sum is the
+    49-bit floor cut, and the byte-permute FP16 route (1024 + offset digit)
+    minus 1024 + offset reproduces every digit exactly."""
+    assert exact_report["exact_cut_bad"] == 0
+    assert exact_report["exact_digit_bad"] == 0
+
+
+def test_exact_operand_and_accumulators(exact_report):
+    """The library's B operand holds integer digits |f| <= 128, and every
+    emulated FP32 accumulator of a pass stays below 2^22 (exact, and in the
+    range of the recombination's magic-number conversion)."""
+    assert exact_report["exact_b_max"] <= 128
+    assert exact_report["exact_acc_max"] < 2 ** 22
+    # seeded with 1.5 * 2^23, every accumulator is an exact FP32 integer
+    assert exact_report["exact_acc_inexact"] == 0
+
+
+def test_exact_pass_matches_dft(exact_report):
+    """A radix-16 pass emulated on the kernel's operand layout (twelve MMAs,
+    integer recombination) matches the 16-point DFT in long double to the
+    49-bit cut: error below 2^-46 of the pass's output bound, and outputs
+    stay below the 2^58.5 bound the next pass relies on."""
+    assert exact_report["exact_pass_err"] < 2.0 ** -46
+    assert exact_report["exact_out_log2"] <= 58.5
