@@ -67,8 +67,9 @@ struct ExactPlan {
   static constexpr int THREADS = 2 * ROWS;  // two threads per row
   static_assert(P == 16 && PL::R[0] == 16, "radix-16 first pass, 16 points per butterfly row");
   static_assert(T * TPB == ROWS, "one row per radix-16 butterfly");
-  static constexpr int B = FxBits<N>::B;  // bound of the first pass's inputs
-  static_assert(B >= 48, "the 49-bit cut needs B >= 48");
+  // inputs are converted to block fixed point below 2^48: the first pass's
+  // 49-bit cut is then the converted value itself (floor of a floor)
+  static constexpr int B = 48;
   static constexpr int KC = 8;                        // 16-byte K chunks per operand row (64 FP16)
   static constexpr int A_BLOCK = 128 * KC * 16;       // 16 KB: one digit pair of 128 rows
   static constexpr int A_BYTES = G * kExactBlocks * A_BLOCK;
@@ -155,9 +156,31 @@ FFTOC_HD long long exact_combine(unsigned x0, unsigned x1, unsigned x2, unsigned
   return (long long)(((unsigned long long)pb << 16) + pc + ((unsigned long long)pa << 32) - KC);
 }
 
-// Six 8-column TMEM loads (one per order, 32 columns apart) and the
-// wait for them, in one statement so that no use of the values can be
-// scheduled before the wait.
+// Six 4-column TMEM loads (one per order, 32 columns apart) and the wait
+// for them, in one statement so that no use of the values can be scheduled
+// before the wait.
+__device__ __forceinline__ void exact_tmem_ld6x4(unsigned taddr, unsigned (&v)[kExactOrders][4]) {
+  unsigned r[24];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%24];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%4,%5,%6,%7}, [%25];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%8,%9,%10,%11}, [%26];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%12,%13,%14,%15}, [%27];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%16,%17,%18,%19}, [%28];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%20,%21,%22,%23}, [%29];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23])
+      : "r"(taddr), "r"(taddr + 32), "r"(taddr + 64), "r"(taddr + 96), "r"(taddr + 128), "r"(taddr + 160)
+      : "memory");
+#pragma unroll
+  for (int s = 0; s < kExactOrders; ++s)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[s][i] = r[4 * s + i];
+}
+
+// The same with 8 columns per order.
 __device__ __forceinline__ void exact_tmem_ld6x8(unsigned taddr, unsigned (&v)[kExactOrders][8]) {
   unsigned r[48];
   asm volatile(
@@ -222,7 +245,7 @@ struct ExactCtx {
   unsigned tmem;            // this group's accumulators, lane 0
   unsigned tmem_rd;         // this thread's lanes and columns
   unsigned phase;
-  int tid, h, row, j, t;
+  int tid, g, h, row, j, t;
   bool issuer, failed;
   const double2* nsrc;  // this thread's first input of the next tile
   bool nactive;         // the next tile holds this thread's transform
@@ -233,6 +256,26 @@ template <int T>
 __device__ __forceinline__ void exact_load_inputs(double2 (&raw)[8], const double2* src, bool active) {
 #pragma unroll
   for (int i = 0; i < 8; ++i) raw[i] = active ? __ldg(src + T * i) : make_double2(0.0, 0.0);
+}
+
+// Passes whose twiddles are loaded into registers before the barrier that
+// precedes them: a radix-16 last pass after another radix-16 pass (measured
+// 4 % faster at N = 256; loading the twiddles of earlier passes ahead, or
+// into an array at all, measured 2-3 % slower at N = 512 and 4096 than
+// loading each at its product).
+template <class PL, int s>
+constexpr bool EARLY_TW = s > 0 && s == PL::S - 1 && PL::R[s] == 16;
+
+// The twiddles of radix-16 pass s (s >= 1) for this thread's inputs
+// m = 8h + i: entry (m - 1) p + k (none for m = 0).
+template <class PL, int s>
+__device__ __forceinline__ void exact_load_twiddles(const ExactCtx& c, int4 (&w)[8]) {
+  constexpr int p = PL::span(s);
+  const int k = c.t & (p - 1);
+  const int4* base = c.tw + PL::tw_offset(s) + k + 8 * c.h * p;
+#pragma unroll
+  for (int i = 1; i < 8; ++i) w[i] = __ldg(base + (i - 1) * p);
+  w[0] = c.h ? __ldg(base - p) : w[1];
 }
 
 template <int R, int Bq, int... bs>
@@ -251,7 +294,7 @@ __device__ __forceinline__ void exact_small_dfts(long long (&re)[8], long long (
 // overlaps the pass.
 template <class PL, int G, int s>
 __device__ __forceinline__ void exact_pass(ExactCtx& c, long long (&re)[8], long long (&im)[8], const ExactOut& o,
-                                           double2 (&raw)[8]) {
+                                           double2 (&raw)[8], const int4 (&w)[8]) {
   using XP = ExactPlan<PL, G>;
   constexpr int T = PL::T, NS = PL::S;
   constexpr int R = PL::R[s];
@@ -270,11 +313,17 @@ __device__ __forceinline__ void exact_pass(ExactCtx& c, long long (&re)[8], long
         re[i] = v.x;
         im[i] = v.y;
       }
-      const int k = c.t & (p - 1);
-      const int4* base = c.tw + PL::tw_offset(s) + k + (8 * c.h - 1) * p;  // input m = 8h + i: (m - 1) p
+      if constexpr (EARLY_TW<PL, s>) {
 #pragma unroll
-      for (int i = 1; i < 8; ++i) EngFx::cmul(re[i], im[i], __ldg(base + i * p));
-      if (c.h) EngFx::cmul(re[0], im[0], __ldg(base));
+        for (int i = 1; i < 8; ++i) EngFx::cmul(re[i], im[i], w[i]);
+        if (c.h) EngFx::cmul(re[0], im[0], w[0]);
+      } else {
+        const int k = c.t & (p - 1);
+        const int4* base = c.tw + PL::tw_offset(s) + k + (8 * c.h - 1) * p;  // input m = 8h + i: (m - 1) p
+#pragma unroll
+        for (int i = 1; i < 8; ++i) EngFx::cmul(re[i], im[i], __ldg(base + i * p));
+        if (c.h) EngFx::cmul(re[0], im[0], __ldg(base));
+      }
     }
     // A digits: values 8h..8h+7 (real) are chunks 2h, 2h+1 of each block,
     // values 16+8h..23+8h (imaginary) chunks 4+2h, 5+2h
@@ -296,7 +345,10 @@ __device__ __forceinline__ void exact_pass(ExactCtx& c, long long (&re)[8], long
     exact_tmem_fill(c.tmem_rd);
     fence_proxy_async_smem();
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
+    // the group's MMAs read only its own rows: a barrier over the group
+    if constexpr (G == 1) __syncthreads();
+    else if (c.g == 0) asm volatile("bar.sync 1, 256;" ::: "memory");
+    else asm volatile("bar.sync 2, 256;" ::: "memory");
     if (c.issuer) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const unsigned a0 = smem_u32(c.sA), b0 = smem_u32(c.sB);
@@ -318,17 +370,21 @@ __device__ __forceinline__ void exact_pass(ExactCtx& c, long long (&re)[8], long
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     // outputs C = (sum_k x_k F_k) 2^(54 - BS), modulus <= 2^58.5
     const int k = c.t & (p - 1);
+    // rounds of WC columns (WC / 2 outputs) per order: 8 with one group, 4
+    // with two (the register budget of 512 threads)
+    constexpr int WC = G == 1 ? 8 : 4;
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
-      unsigned v[kExactOrders][8];
-      exact_tmem_ld6x8(c.tmem_rd + 8 * r, v);
+    for (int r = 0; r < 16 / WC; ++r) {
+      unsigned v[kExactOrders][WC];
+      if constexpr (WC == 8) exact_tmem_ld6x8(c.tmem_rd + WC * r, v);
+      else exact_tmem_ld6x4(c.tmem_rd + WC * r, v);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < WC / 2; ++q) {
         const long long yr = exact_combine(v[0][2 * q], v[1][2 * q], v[2][2 * q], v[3][2 * q], v[4][2 * q],
                                            v[5][2 * q]);
         const long long yi = exact_combine(v[0][2 * q + 1], v[1][2 * q + 1], v[2][2 * q + 1], v[3][2 * q + 1],
                                            v[4][2 * q + 1], v[5][2 * q + 1]);
-        const int m = 8 * c.h + 4 * r + q;
+        const int m = 8 * c.h + (WC / 2) * r + q;
         const int e = (c.t - k) * 16 + k + m * p;
         if constexpr (s + 1 < NS) c.data[XP::slot(c.j, e)] = make_longlong2(yr, yi);
         else if (o.active) o.dst[e] = exact_out_value(o, yr, yi);
@@ -349,8 +405,7 @@ __device__ __forceinline__ void exact_pass(ExactCtx& c, long long (&re)[8], long
 #pragma unroll
     for (int b = 0; b < Bh; ++b) {
       const int tp = c.t + T * (c.h * Bh + b);
-      const int k = tp & (p - 1);
-      const int4* base = c.tw + PL::tw_offset(s) + k;
+      const int4* base = c.tw + PL::tw_offset(s) + (tp & (p - 1));
 #pragma unroll
       for (int m = 1; m < R; ++m) EngFx::cmul(re[b + Bh * m], im[b + Bh * m], __ldg(base + (m - 1) * p));
     }
@@ -367,16 +422,28 @@ __device__ __forceinline__ void exact_pass(ExactCtx& c, long long (&re)[8], long
     }
   }
   if constexpr (s + 1 < NS) {
+    int4 wn[8];
+    if constexpr (EARLY_TW<PL, s + 1>) exact_load_twiddles<PL, s + 1>(c, wn);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    exact_pass<PL, G, s + 1>(c, re, im, o, raw);
+    exact_pass<PL, G, s + 1>(c, re, im, o, raw, wn);
   }
 }
 
-// Largest value of a over a transform's rows and both halves: shuffles within
-// the warp, one word per (transform, half, warp) in `red`, one barrier.
+// Largest sign-cleared high word of a thread's inputs: the exponent field
+// of its largest value, or for subnormals the position of the leading bit.
+__device__ __forceinline__ unsigned exact_high_max(const double2 (&raw)[8]) {
+  unsigned a = 0u;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) a = max(a, max(hi_word(raw[i].x) & 0x7FFFFFFFu, hi_word(raw[i].y) & 0x7FFFFFFFu));
+  return a;
+}
+
+// Largest value of a over a transform's rows and both halves, in two steps
+// around a barrier: shuffles within the warp and one word per (transform,
+// half, warp) in `red`; after the barrier, the maximum of the transform's words.
 template <int T, int TPB, int W>
-__device__ __forceinline__ unsigned exact_transform_max(unsigned a, int h, int j, int t, unsigned* red) {
+__device__ __forceinline__ void exact_transform_put(unsigned a, int h, int j, int t, unsigned* red) {
   if constexpr (T >= 32) {
     a = __reduce_max_sync(0xffffffffu, a);
   } else if constexpr (T > 1) {
@@ -384,8 +451,10 @@ __device__ __forceinline__ unsigned exact_transform_max(unsigned a, int h, int j
     for (int o = T / 2; o > 0; o >>= 1) a = max(a, __shfl_xor_sync(0xffffffffu, a, o, T));
   }
   if ((t & 31) == 0) red[(h * TPB + j) * W + (t >> 5)] = a;
-  __syncthreads();
-  a = red[j * W];
+}
+template <int TPB, int W>
+__device__ __forceinline__ unsigned exact_transform_get(int j, const unsigned* red) {
+  unsigned a = red[j * W];
 #pragma unroll
   for (int w = 1; w < 2 * W; ++w) a = max(a, red[((w / W) * TPB + j) * W + (w % W)]);
   return a;
@@ -414,6 +483,7 @@ fft_exact_kernel(const double2* __restrict__ in, double2* __restrict__ out, long
   c.bar = bars + g;
   c.tw = tw;
   c.tid = tid;
+  c.g = g;
   c.h = h;
   c.row = row;
   c.j = grow / T;
@@ -426,6 +496,14 @@ fft_exact_kernel(const double2* __restrict__ in, double2* __restrict__ out, long
   if (tid == 0) {
     for (int gg = 0; gg < G; ++gg) mbar_init(bars + gg, 1);
     mbar_fence_init();
+  }
+  // the first tile's inputs and maximum (read after the set-up barrier)
+  const long long ntiles = (batch + TPB - 1) / TPB;
+  double2 raw[8];  // the current tile's inputs, loaded during the previous tile
+  {
+    const long long tr = (long long)blockIdx.x * TPB + c.j;
+    exact_load_inputs<T>(raw, in + (tr < batch ? tr : 0) * N + c.t + T * 8 * h, tr < batch);
+    exact_transform_put<T, TPB, XP::W>(exact_high_max(raw), h, c.j, c.t, red);
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
@@ -442,12 +520,6 @@ fft_exact_kernel(const double2* __restrict__ in, double2* __restrict__ out, long
   c.tmem_rd = c.tmem + ((unsigned)((warp & 3) * 32) << 16) + 16 * h;
   c.phase = 0;
 
-  const long long ntiles = (batch + TPB - 1) / TPB;
-  double2 raw[8];  // the current tile's inputs, loaded during the previous tile
-  if (blockIdx.x < ntiles) {
-    const long long tr = (long long)blockIdx.x * TPB + c.j;
-    exact_load_inputs<T>(raw, in + tr * N + c.t + T * 8 * h, tr < batch);
-  }
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     if (tid == 0) prefetch_next_tile<N, TPB>(in, tile, batch);
     const long long tr = tile * TPB + c.j;
@@ -455,13 +527,10 @@ fft_exact_kernel(const double2* __restrict__ in, double2* __restrict__ out, long
     const long long ntr = tr + (long long)gridDim.x * TPB;
     c.nactive = ntr < batch;
     c.nsrc = in + (c.nactive ? ntr : 0) * N + c.t + T * 8 * h;
-    // the transform's largest sign-cleared high word: its exponent field, or
-    // for a transform of subnormals (field 0) the position of its leading bit
-    unsigned amax = 0u;
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-      amax = max(amax, max(hi_word(raw[i].x) & 0x7FFFFFFFu, hi_word(raw[i].y) & 0x7FFFFFFFu));
-    const unsigned at = exact_transform_max<T, TPB, XP::W>(amax, h, c.j, c.t, red);
+    // the transform's largest sign-cleared high word (put before the previous
+    // barrier): its exponent field, or for a transform of subnormals (field
+    // 0) the position of its leading bit
+    const unsigned at = exact_transform_get<TPB, XP::W>(c.j, red);
     int em = (int)(at >> 20), kadj = 0;
     if (em == 0 && at != 0u) {
       // subnormal transform (largest value in [2^-1074 2^32, 2^-1022)): scale
@@ -481,7 +550,10 @@ fft_exact_kernel(const double2* __restrict__ in, double2* __restrict__ out, long
     const int e_out = (em < 1 ? 1 : em) + XP::OUT_SHIFT + kadj, k_out = sc.K + XP::OUT_SHIFT + kadj;
     const ExactOut o{out + tr * N, active, e_out < XP::B || e_out > 1983 + XP::B, sc.special,
                      (int)((unsigned)k_out << 20), k_out};
-    exact_pass<PL, G, 0>(c, re, im, o, raw);
+    const int4 w0[8] = {};
+    exact_pass<PL, G, 0>(c, re, im, o, raw, w0);
+    // the next tile's maximum, read after the barrier
+    exact_transform_put<T, TPB, XP::W>(exact_high_max(raw), h, c.j, c.t, red);
     if (__syncthreads_or(c.failed)) {
       if (tid == 0) atomicOr(err, kErrTimeout);
       mbar_wait_bounded(c.bar, c.phase ^ 1, kWaitLimitNs);  // bounded drain of the MMAs in flight

@@ -140,9 +140,8 @@ int main() {
     if (v != std::floor(v)) bmax = 1e9;
     bmax = std::fmax(bmax, std::fabs(v));
   }
-  check_pass<49>(g, bop, 300);  // N = 4096, first pass
-  check_pass<53>(g, bop, 300);  // N <= 256, first pass
-  check_pass<59>(g, bop, 300);  // later passes
+  check_pass<48>(g, bop, 400);  // first pass (inputs converted below 2^48)
+  check_pass<59>(g, bop, 400);  // later passes
   std::printf("exact_cut_bad %g\n", g_cut_bad);
   std::printf("exact_digit_bad %g\n", g_digit_bad);
   std::printf("exact_b_max %g\n", bmax);
