@@ -396,6 +396,21 @@ struct IndexedTile {
   __device__ __forceinline__ static double2 load(const double2* p) { return __ldg(p); }
 };
 
+// Tiles of an uneven batch for plans that do not stage their tile (each
+// thread touches only its own transform): the thread's transform offset in a
+// register, loaded ahead by the caller.
+struct RegTile {
+  const double2* __restrict__ in;
+  double2* __restrict__ out;
+  long long off;  // this thread's transform
+  long long tile0, count;
+  __device__ __forceinline__ const double2* in_of(int) const { return in + off; }
+  __device__ __forceinline__ double2* out_of(int) const { return out + off; }
+  __device__ __forceinline__ const double2* in_elem(int, int, int e) const { return in + off + e; }
+  __device__ __forceinline__ double2* out_elem(int, int, int e) const { return out + off + e; }
+  __device__ __forceinline__ static double2 load(const double2* p) { return __ldg(p); }
+};
+
 // The on-chip repeat harness: the tile's transforms resident in shared
 // memory (`buf`, TPB * N points, transformed in place), loaded with plain
 // shared loads.

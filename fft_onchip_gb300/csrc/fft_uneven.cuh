@@ -140,42 +140,70 @@ static __global__ void __launch_bounds__(kUnevenChunk) uneven_scatter(UnevenArgs
         __ldg(a->offsets + i);
 }
 
+// Slots of the per-CTA ring of tile offsets (current, next, the one after).
+constexpr int kUnevenRing = 3;
+
 // Persistent per-size kernel: CTAs stride over the tiles of bucket `bin`.
+// The tiles' transform offsets pass through a ring of kUnevenRing slots in
+// shared memory, filled with cp.async two tiles ahead: no offset is held in a
+// register across a tile (the plans run at their register limit), the L2
+// prefetch of the next tile reads its offsets from the ring, and one barrier
+// per tile makes the slots visible.  Plans that do not stage their tile read
+// their own transform's offset once; staged plans index the slot.
 template <class E, class PL>
 __global__ void __launch_bounds__(Fft<E, PL>::THREADS, PL::MINB)
 fft_uneven_kernel(const UnevenArgs* __restrict__ a, int bin, const typename E::TW* __restrict__ tw) {
   using F = Fft<E, PL>;
+  using FK = Fft<PlanEngine<E, PL>, PL>;
   constexpr int TPB = PL::TPB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  long long* base = reinterpret_cast<long long*>(smem_raw + F::SMEM);
+  long long* ring = reinterpret_cast<long long*>(smem_raw + F::SMEM);  // [kUnevenRing][TPB]
   const long long count = a->bucket_count[bin];
+  // tiles of the bucket, counted in 32 bits (the loop state stays small: the
+  // plans run at their register limit)
+  const int ntiles = (int)((count + TPB - 1) / TPB);
+  if ((int)blockIdx.x >= ntiles) return;
   const long long* list = a->list + a->bucket_start[bin];
-  const IndexedTile proto{a->in, a->out, base, 0, count};
-  const long long stride = (long long)gridDim.x * TPB;
-  // offset of this thread's transform in the current tile; the next tile's is
-  // loaded one iteration ahead, with its L2 prefetch
-  long long cur = 0;
-  if (threadIdx.x < TPB) {
-    const long long k = (long long)blockIdx.x * TPB + threadIdx.x;
-    cur = k < count ? __ldg(list + k) : 0;
+  const int tid = threadIdx.x;
+  // offset of the bucket's transform k (0 past the end) into ring slot `slot`
+  auto fetch = [&](int slot, long long k) {
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(ring + slot * TPB + tid);
+    const bool in = k < count;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(list + (in ? k : 0)),
+                 "r"(in ? 8 : 0)
+                 : "memory");
+  };
+  if (tid < TPB) {
+    fetch(0, (long long)blockIdx.x * TPB + tid);
+    fetch(1, (long long)(blockIdx.x + gridDim.x) * TPB + tid);
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_all;" ::: "memory");
   }
-  for (long long tile0 = (long long)blockIdx.x * TPB; tile0 < count; tile0 += stride) {
-    __syncthreads();  // the previous tile's readers of `base` and the staging buffer are done
-    if (threadIdx.x < TPB) {
-      base[threadIdx.x] = cur;
+  __syncthreads();
+  int s0 = 0;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long tile0 = (long long)tile * TPB;
+    const int s1 = s0 == kUnevenRing - 1 ? 0 : s0 + 1, s2 = s1 == kUnevenRing - 1 ? 0 : s1 + 1;
+    if (tid < TPB) {
+      fetch(s2, (long long)(tile + 2 * (int)gridDim.x) * TPB + tid);
+      asm volatile("cp.async.commit_group;" ::: "memory");
       // this CTA's next tile, transform by transform, into L2
-      const long long kn = tile0 + threadIdx.x + stride;
-      cur = 0;
-      if (kn < count) {
-        cur = __ldg(list + kn);
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a->in + cur), "r"((unsigned)(PL::N * 16))
+      if ((long long)(tile + (int)gridDim.x) * TPB + tid < count)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a->in + ring[s1 * TPB + tid]),
+                     "r"((unsigned)(PL::N * 16))
                      : "memory");
-      }
     }
+    if constexpr (!FK::STAGED) {
+      const RegTile tl{a->in, a->out, ring[s0 * TPB + tid / FK::T], tile0, count};
+      fft_tile<E, PL>(tl, tw, smem_raw);
+    } else {
+      const IndexedTile tl{a->in, a->out, ring + s0 * TPB, tile0, count};
+      fft_tile<E, PL>(tl, tw, smem_raw);
+    }
+    if (tid < TPB) asm volatile("cp.async.wait_all;" ::: "memory");
+    // the ring slot filled above is visible, and this tile's readers of the
+    // exchange buffer and of slot s0 are done
     __syncthreads();
-    IndexedTile tl = proto;
-    tl.tile0 = tile0;
-    fft_tile<E, PL>(tl, tw, smem_raw);
+    s0 = s1;
   }
 }
 
