@@ -140,6 +140,15 @@ class UnevenPlan:
                      stream.cuda_stream))
         return out
 
+    def device_sized(self):
+        """True when the graph sizes its per-size kernels on the device (one CTA
+        per tile), False when it runs persistent per-size kernels."""
+        import ctypes
+
+        v = ctypes.c_int(0)
+        check(self._L.fftoc_uneven_plan_device_sized(self._p, ctypes.byref(v)))
+        return bool(v.value)
+
     def counts(self):
         """Per-size transform counts of the last bucketing {n: count}."""
         import ctypes

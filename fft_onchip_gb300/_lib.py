@@ -50,6 +50,7 @@ EXPORTS = tuple(["fftoc_c2c_fwd_n%d" % n for n in SIZES]) + (
     "fftoc_uneven_execute",
     "fftoc_uneven_execute_per_size",
     "fftoc_uneven_counts",
+    "fftoc_uneven_plan_device_sized",
     "fftoc_uneven_plan_destroy",
     "fftoc_c2c_fwd_uneven",
     "fftoc_server_config_default",
@@ -168,6 +169,8 @@ def load(path=None):
         f.restype = c_int
     L.fftoc_uneven_counts.argtypes = [vp, ctypes.POINTER(i64)]
     L.fftoc_uneven_counts.restype = c_int
+    L.fftoc_uneven_plan_device_sized.argtypes = [vp, ctypes.POINTER(c_int)]
+    L.fftoc_uneven_plan_device_sized.restype = c_int
     L.fftoc_uneven_plan_destroy.argtypes = [vp]
     L.fftoc_uneven_plan_destroy.restype = c_int
     L.fftoc_c2c_fwd_uneven.argtypes = [vp, vp, vp, vp, i64, vp]

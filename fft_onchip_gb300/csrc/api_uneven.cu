@@ -34,6 +34,7 @@ struct fftoc_uneven_plan_s {
   cudaEvent_t join[fftoc::kNumSizes] = {};
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  bool device_sized = false;  // the graph's size kernels get their grids from uneven_scan
   std::mutex mu;
 };
 
@@ -148,23 +149,47 @@ fftoc_status resolve_kernels(fftoc_uneven_plan p, const UnevenDevice& u, bool* c
   return FFTOC_OK;
 }
 
-fftoc_status enqueue_bucketing(fftoc_uneven_plan p, cudaStream_t s) {
+fftoc_status enqueue_bucketing(fftoc_uneven_plan p, cudaStream_t s, bool size_nodes) {
   uneven_hist<<<p->chunks, kUnevenChunk, 0, s>>>(p->args, p->err);
-  uneven_scan<<<1, 32 * kUnevenBins, 0, s>>>(p->args);
+  uneven_scan<<<1, 32 * kUnevenBins, 0, s>>>(p->args, size_nodes ? 1 : 0);
   uneven_scatter<<<p->chunks, kUnevenChunk, 0, s>>>(p->args);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? FFTOC_OK : cuda_err(e, "bucketing launch");
 }
 
-fftoc_status launch_size(fftoc_uneven_plan p, int i, long long blocks, cudaStream_t s) {
+// Launch of size i's kernel; with `node` (during capture) as a
+// device-updatable graph node whose handle is returned there.
+fftoc_status launch_size(fftoc_uneven_plan p, int i, long long blocks, cudaStream_t s,
+                         cudaGraphDeviceNode_t* node = nullptr) {
   const KernelDesc& d = *p->kd[i];
   UnevenArgs* a = p->args;
   int bin = i;
   const void* tw = p->tw[i];
   void* kargs[] = {(void*)&a, (void*)&bin, (void*)&tw};
-  cudaError_t e = cudaLaunchKernel(d.fn_uneven, dim3((unsigned)blocks), dim3(d.threads), kargs,
-                                   (size_t)d.smem_uneven, s);
+  cudaError_t e;
+  if (node) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(d.threads);
+    cfg.dynamicSmemBytes = (size_t)d.smem_uneven;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeDeviceUpdatableKernelNode;
+    attr[0].val.deviceUpdatableKernelNode.deviceUpdatable = 1;
+    attr[0].val.deviceUpdatableKernelNode.devNode = nullptr;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelExC(&cfg, d.fn_uneven, kargs);
+    *node = attr[0].val.deviceUpdatableKernelNode.devNode;
+    if (e == cudaSuccess && *node == nullptr) e = cudaErrorInvalidValue;
+  } else {
+    e = cudaLaunchKernel(d.fn_uneven, dim3((unsigned)blocks), dim3(d.threads), kargs, (size_t)d.smem_uneven, s);
+  }
   return e == cudaSuccess ? FFTOC_OK : cuda_err(e, "cudaLaunchKernel(uneven)");
+}
+
+long long wave_blocks(fftoc_uneven_plan p, int i) {
+  return (long long)p->sms * p->kd[i]->blocks_per_sm_uneven;
 }
 
 long long persistent_blocks(fftoc_uneven_plan p, int i) {
@@ -174,7 +199,11 @@ long long persistent_blocks(fftoc_uneven_plan p, int i) {
   return tiles < cap ? tiles : cap;
 }
 
-fftoc_status capture(fftoc_uneven_plan p) {
+// One capture attempt: bucketing, then one kernel per size on its own
+// branch.  With `size_nodes` the size kernels are device-updatable nodes whose
+// grids uneven_scan sets on every launch; their handles, transforms per CTA
+// and wave sizes go to the argument block.
+fftoc_status capture_once(fftoc_uneven_plan p, bool size_nodes) {
   if (p->exec) {
     cudaGraphExecDestroy(p->exec);
     p->exec = nullptr;
@@ -185,14 +214,16 @@ fftoc_status capture(fftoc_uneven_plan p) {
   }
   cudaError_t e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return cuda_err(e, "cudaStreamBeginCapture");
-  fftoc_status st = enqueue_bucketing(p, p->cap);
+  cudaGraphDeviceNode_t nodes[kUnevenBins] = {};
+  fftoc_status st = enqueue_bucketing(p, p->cap, size_nodes);
   if (st == FFTOC_OK && (e = cudaEventRecord(p->fork, p->cap)) != cudaSuccess) st = cuda_err(e, "cudaEventRecord");
+  // every size on its own branch: the sizes run side by side
   for (int i = 0; i < kNumSizes && st == FFTOC_OK; ++i) {
     if ((e = cudaStreamWaitEvent(p->branch[i], p->fork, 0)) != cudaSuccess) {
       st = cuda_err(e, "cudaStreamWaitEvent");
       break;
     }
-    st = launch_size(p, i, persistent_blocks(p, i), p->branch[i]);
+    st = launch_size(p, i, persistent_blocks(p, i), p->branch[i], size_nodes ? &nodes[i] : nullptr);
     if (st != FFTOC_OK) break;
     if ((e = cudaEventRecord(p->join[i], p->branch[i])) != cudaSuccess) st = cuda_err(e, "cudaEventRecord");
     else if ((e = cudaStreamWaitEvent(p->cap, p->join[i], 0)) != cudaSuccess) st = cuda_err(e, "cudaStreamWaitEvent");
@@ -207,7 +238,35 @@ fftoc_status capture(fftoc_uneven_plan p) {
   p->graph = g;
   e = cudaGraphInstantiate(&p->exec, g, 0);
   if (e != cudaSuccess) return cuda_err(e, "cudaGraphInstantiate");
+  // a graph that updates its own nodes from the device is uploaded before
+  // its first launch
+  if (size_nodes && (e = cudaGraphUpload(p->exec, p->cap)) == cudaSuccess) e = cudaStreamSynchronize(p->cap);
+  if (e != cudaSuccess) return cuda_err(e, "cudaGraphUpload");
+  int tpb[kUnevenBins] = {}, wave[kUnevenBins] = {};
+  for (int i = 0; i < kNumSizes; ++i) {
+    tpb[i] = p->kd[i]->tpb;
+    wave[i] = (int)wave_blocks(p, i);
+  }
+  char* a = reinterpret_cast<char*>(p->args);
+  if ((e = cudaMemcpy(a + offsetof(UnevenArgs, nodes), nodes, sizeof(nodes), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(a + offsetof(UnevenArgs, tpb), tpb, sizeof(tpb), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(a + offsetof(UnevenArgs, wave), wave, sizeof(wave), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_err(e, "cudaMemcpy(uneven graph nodes)");
+  p->device_sized = size_nodes;
   return FFTOC_OK;
+}
+
+// Captures the plan's graph with device-sized grids, or with persistent grids
+// where the runtime refuses device-updatable nodes.  A re-capture first waits
+// for the device: executions of the previous graph read the argument block.
+fftoc_status capture(fftoc_uneven_plan p) {
+  if (p->exec) {
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_err(e, "cudaDeviceSynchronize");
+  }
+  if (capture_once(p, true) == FFTOC_OK) return FFTOC_OK;
+  cudaGetLastError();
+  return capture_once(p, false);
 }
 
 void release(fftoc_uneven_plan p) {
@@ -340,7 +399,7 @@ fftoc_status execute_per_size(fftoc_uneven_plan p, const double* in, double* out
   bool changed = false;
   if ((st = resolve_kernels(p, *u, &changed)) != FFTOC_OK) return st;
   if ((st = set_args(p, in, out, offsets, ns, count, s)) != FFTOC_OK) return st;
-  if ((st = enqueue_bucketing(p, s)) != FFTOC_OK) return st;
+  if ((st = enqueue_bucketing(p, s, false)) != FFTOC_OK) return st;
   int h[kNumSizes];
   if ((st = read_counts(p, h, s)) != FFTOC_OK) return st;
   for (int i = 0; i < kNumSizes; ++i) {
@@ -375,6 +434,13 @@ fftoc_status fftoc_uneven_execute_per_size(fftoc_uneven_plan plan, const double*
                                            const int64_t* offsets, const int32_t* ns, int64_t count,
                                            fftoc_stream stream) {
   return fftoc::execute_per_size(plan, in, out, offsets, ns, count, (cudaStream_t)stream);
+}
+
+fftoc_status fftoc_uneven_plan_device_sized(fftoc_uneven_plan plan, int* sized) {
+  if (!plan || !sized) return fftoc::set_error(FFTOC_ERR_INVALID_VALUE, "null pointer");
+  std::lock_guard<std::mutex> lk(plan->mu);
+  *sized = plan->device_sized ? 1 : 0;
+  return FFTOC_OK;
 }
 
 fftoc_status fftoc_uneven_counts(fftoc_uneven_plan plan, int64_t* counts) {

@@ -9,11 +9,16 @@
 //   2. uneven_scan     bucket starts and per-chunk bases (one CTA);
 //   3. uneven_scatter  stable bucketing: transform offsets grouped by size, in
 //                      table order within a size;
-//   4. fft_uneven_kernel<E, PL>, one per size on parallel graph branches:
-//      persistent CTAs walk their size's bucket tile by tile, loading each
-//      transform from its own offset.
-// Steps 1-3 read the transform count from device memory, so the graph's
-// launch geometry depends only on the plan's maximum count.
+//   4. fft_uneven_kernel<E, PL>, one per size on parallel graph branches,
+//      each CTA loading its transforms from their own offsets.
+// Steps 1-3 read the transform count from device memory.  The size kernels
+// are device-updatable graph nodes whose grids uneven_scan sets from the
+// bucket counts: one CTA per tile (like the batched kernels) for a size that
+// has nearly the whole batch, else persistent grids of the size's resident
+// CTAs, the sizes side by side on parallel branches.  Where
+// the runtime refuses device-updatable nodes, the graph keeps persistent
+// grids (the SM count times the resident CTAs) and the CTAs walk their
+// bucket tile by tile.
 #pragma once
 #include "fft_kernel.cuh"
 #include "internal.h"
@@ -36,6 +41,12 @@ struct UnevenArgs {
   int* chunk_base;            // [chunks][kUnevenBins]
   int bucket_count[kUnevenBins];
   int bucket_start[kUnevenBins];
+  // per size, set when the graph is captured: the size kernel's node (null
+  // where the graph has persistent grids), its transforms per CTA, and its
+  // resident CTAs on the device (the L2 prefetch distance)
+  cudaGraphDeviceNode_t nodes[kUnevenBins];
+  int tpb[kUnevenBins];
+  int wave[kUnevenBins];
 };
 
 static __global__ void uneven_set_args(UnevenArgs* a, const double2* in, double2* out, const long long* offsets,
@@ -76,7 +87,9 @@ static __global__ void __launch_bounds__(kUnevenChunk) uneven_hist(UnevenArgs* _
 }
 
 // One CTA of 32 x kUnevenBins threads: warp b scans bin b over the chunks.
-static __global__ void __launch_bounds__(32 * kUnevenBins) uneven_scan(UnevenArgs* __restrict__ a) {
+// With `size_nodes` (launched from the graph), the size kernels' grids are
+// set from the bucket counts.
+static __global__ void __launch_bounds__(32 * kUnevenBins) uneven_scan(UnevenArgs* __restrict__ a, int size_nodes) {
   __shared__ int total[kUnevenBins];
   const int bin = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long count = a->count;
@@ -103,6 +116,22 @@ static __global__ void __launch_bounds__(32 * kUnevenBins) uneven_scan(UnevenArg
       a->bucket_count[b] = b < kUnevenInvalid ? total[b] : 0;
       s += total[b];
     }
+  }
+  if (size_nodes && threadIdx.x < kUnevenInvalid && a->nodes[threadIdx.x] != nullptr) {
+    // A size with nearly all of the batch's bytes runs one CTA per tile
+    // (measured 9-15 % faster alone at N = 512..4096).  Sizes that share the
+    // batch keep persistent grids of their resident CTAs on the device, so
+    // that each can use the whole device as the others finish (measured
+    // faster on mixed batches than one CTA per tile, whose grids then run
+    // one after another, and than grids in proportion to each size's bytes).
+    const int b = threadIdx.x;
+    double bytes = 0.0;
+    for (int i = 0; i < kUnevenInvalid; ++i) bytes += (double)total[i] * (double)(8 << i);
+    const double share = bytes > 0.0 ? (double)total[b] * (double)(8 << b) / bytes : 1.0;
+    const int tpb = a->tpb[b];
+    const long long tiles = ((long long)total[b] + tpb - 1) / tpb;
+    const long long grid = share >= 0.9 || tiles < a->wave[b] ? tiles : a->wave[b];
+    cudaGraphKernelNodeSetGridDim(a->nodes[b], dim3(grid > 0 ? (unsigned)grid : 1u));
   }
 }
 
@@ -143,13 +172,15 @@ static __global__ void __launch_bounds__(kUnevenChunk) uneven_scatter(UnevenArgs
 // Slots of the per-CTA ring of tile offsets (current, next, the one after).
 constexpr int kUnevenRing = 3;
 
-// Persistent per-size kernel: CTAs stride over the tiles of bucket `bin`.
-// The tiles' transform offsets pass through a ring of kUnevenRing slots in
-// shared memory, filled with cp.async two tiles ahead: no offset is held in a
-// register across a tile (the plans run at their register limit), the L2
-// prefetch of the next tile reads its offsets from the ring, and one barrier
-// per tile makes the slots visible.  Plans that do not stage their tile read
-// their own transform's offset once; staged plans index the slot.
+// Per-size kernel: CTAs stride over the tiles of bucket `bin` (one tile each
+// when the grid covers the bucket).  The tiles' transform offsets pass
+// through a ring of kUnevenRing slots in shared memory, filled with cp.async:
+// slot s0 holds the current tile, s1 the tile `ahead` tiles later (this CTA's
+// next tile when the grid is persistent, else the tile one wave of resident
+// CTAs later), whose transforms are prefetched into L2.  No offset is held in
+// a register across a tile (the plans run at their register limit), and one
+// barrier per tile makes the slots visible.  Plans that do not stage their
+// tile read their own transform's offset once; staged plans index the slot.
 template <class E, class PL>
 __global__ void __launch_bounds__(Fft<E, PL>::THREADS, PL::MINB)
 fft_uneven_kernel(const UnevenArgs* __restrict__ a, int bin, const typename E::TW* __restrict__ tw) {
@@ -164,6 +195,11 @@ fft_uneven_kernel(const UnevenArgs* __restrict__ a, int bin, const typename E::T
   const int ntiles = (int)((count + TPB - 1) / TPB);
   if ((int)blockIdx.x >= ntiles) return;
   const long long* list = a->list + a->bucket_start[bin];
+  // a grid that covers the bucket runs one tile per CTA and prefetches one
+  // wave of resident CTAs ahead; a smaller (persistent) grid prefetches the
+  // CTA's next tile, whose offsets the ring then already holds
+  const int wave = a->wave[bin];
+  const int ahead = (int)gridDim.x >= ntiles && wave > 0 && wave < (int)gridDim.x ? wave : (int)gridDim.x;
   const int tid = threadIdx.x;
   // offset of the bucket's transform k (0 past the end) into ring slot `slot`
   auto fetch = [&](int slot, long long k) {
@@ -175,7 +211,7 @@ fft_uneven_kernel(const UnevenArgs* __restrict__ a, int bin, const typename E::T
   };
   if (tid < TPB) {
     fetch(0, (long long)blockIdx.x * TPB + tid);
-    fetch(1, (long long)(blockIdx.x + gridDim.x) * TPB + tid);
+    fetch(1, (long long)(blockIdx.x + ahead) * TPB + tid);
     asm volatile("cp.async.commit_group;\n\tcp.async.wait_all;" ::: "memory");
   }
   __syncthreads();
@@ -184,10 +220,12 @@ fft_uneven_kernel(const UnevenArgs* __restrict__ a, int bin, const typename E::T
     const long long tile0 = (long long)tile * TPB;
     const int s1 = s0 == kUnevenRing - 1 ? 0 : s0 + 1, s2 = s1 == kUnevenRing - 1 ? 0 : s1 + 1;
     if (tid < TPB) {
-      fetch(s2, (long long)(tile + 2 * (int)gridDim.x) * TPB + tid);
-      asm volatile("cp.async.commit_group;" ::: "memory");
-      // this CTA's next tile, transform by transform, into L2
-      if ((long long)(tile + (int)gridDim.x) * TPB + tid < count)
+      if (tile + (int)gridDim.x < ntiles) {  // a next tile of this CTA (persistent grid: ahead = gridDim)
+        fetch(s2, (long long)(tile + 2 * ahead) * TPB + tid);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+      }
+      // the transforms `ahead` tiles later, into L2
+      if ((long long)(tile + ahead) * TPB + tid < count)
         asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a->in + ring[s1 * TPB + tid]),
                      "r"((unsigned)(PL::N * 16))
                      : "memory");
@@ -199,6 +237,7 @@ fft_uneven_kernel(const UnevenArgs* __restrict__ a, int bin, const typename E::T
       const IndexedTile tl{a->in, a->out, ring + s0 * TPB, tile0, count};
       fft_tile<E, PL>(tl, tw, smem_raw);
     }
+    if (tile + (int)gridDim.x >= ntiles) break;  // the last tile of this CTA
     if (tid < TPB) asm volatile("cp.async.wait_all;" ::: "memory");
     // the ring slot filled above is visible, and this tile's readers of the
     // exchange buffer and of slot s0 are done

@@ -223,8 +223,9 @@ fftoc_status fftoc_autotune(int n, int engine, int64_t batch, fftoc_stream strea
  *
  * A plan owns the bucketing scratch (8 bytes per transform plus 64 bytes per
  * 1024) and one CUDA graph: three bucketing kernels that group the transform
- * offsets by size (stable), then one persistent kernel per size on parallel
- * graph branches, each using the plan currently chosen for its size
+ * offsets by size (stable), then one kernel per size on parallel graph
+ * branches, its grid set on the device to the size's tile count (see
+ * fftoc_uneven_plan_device_sized), each using the plan currently chosen for its size
  * (fftoc_plan_select / fftoc_autotune; while a size's choice is the default
  * variant 0 the path uses its own default plan for that size, and
  * TMA-prefetching plans fall back to the size's first plan without prefetch;
@@ -249,6 +250,10 @@ fftoc_status fftoc_uneven_execute_per_size(fftoc_uneven_plan plan, const double 
 /* Per-size transform counts of the last bucketing (counts[10], sizes 8..4096);
  * synchronous. */
 fftoc_status fftoc_uneven_counts(fftoc_uneven_plan plan, int64_t *counts);
+/* *sized = 1 when the plan's graph sizes its per-size kernels on the device
+ * (device-updatable graph nodes: one CTA per tile), 0 when the runtime refused
+ * them and the graph runs persistent per-size kernels. */
+fftoc_status fftoc_uneven_plan_device_sized(fftoc_uneven_plan plan, int *sized);
 fftoc_status fftoc_uneven_plan_destroy(fftoc_uneven_plan plan);
 
 /* One-shot form: a plan cached per device, grown (re-created) when `count`

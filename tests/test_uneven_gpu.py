@@ -89,6 +89,33 @@ def test_mixed_batch_matches_oracle_and_per_size_path(cuda, fftoc_lib, engine):
         assert counts[n] == int(np.sum(ns == n))
     y2 = plan(dev(cuda, xf), dev(cuda, off), dev(cuda, ns), per_size=True).cpu().numpy()
     assert np.array_equal(y2.view(np.uint64), y.view(np.uint64))
+    # the graph sizes its per-size kernels on the device (one CTA per tile)
+    assert plan.device_sized()
+    plan.close()
+    assert F._lib.load().fftoc_device_error_check() == 0
+
+
+def test_device_sized_grids_follow_each_batch(cuda, fftoc_lib):
+    """Back-to-back executions of one plan on batches of different size mixes
+    (so different per-size grids, set on the device by each launch), queued
+    on one stream without synchronising: each output equals the per-size
+    path's on the same batch."""
+    import fft_onchip_gb300 as F
+    plan = F.UnevenPlan(6000)
+    assert plan.device_sized()
+    batches = []
+    for count, seed in ((6000, 31), (40, 32), (2500, 33), (1, 34)):
+        xf, off, ns = workload(count, seed=seed)
+        if count == 1:
+            ns[:] = 4096
+            off, total = inputs.uneven_layout(ns)
+            xf = inputs.uniform_flat(total, seed=seed)
+        batches.append((dev(cuda, xf), dev(cuda, off), dev(cuda, ns)))
+    outs = [plan(x, o, n) for (x, o, n) in batches]  # no synchronisation in between
+    cuda.cuda.synchronize()
+    for (x, o, n), y in zip(batches, outs):
+        ref = plan(x, o, n, per_size=True)
+        assert cuda.equal(bits(y), bits(ref))
     plan.close()
     assert F._lib.load().fftoc_device_error_check() == 0
 
