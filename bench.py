@@ -636,6 +636,7 @@ def bench_uneven(args, torch, F, dev, stream, world):
                      "hbm_gbs": round(algo_bytes / (ms * 1e-3) / 1e9, 1),
                      "frac_hbm": round(algo_bytes / (ms * 1e-3) / 1e9 / hbm, 4)}
     out["graph_speedup_vs_per_size"] = round(out["per_size_launches"]["ms"] / out["graph"]["ms"], 3)
+    out["graph_grids_set_on_device"] = plan.device_sized()
     out["gpu_launches_per_step"] = {"graph": 1 + 3 + len(inputs.SIZES),
                                     "per_size_launches": 1 + 3 + int(sum(1 for n in inputs.SIZES if np.any(ns == n)))}
     plan.close()
