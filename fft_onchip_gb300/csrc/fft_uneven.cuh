@@ -86,6 +86,19 @@ static __global__ void __launch_bounds__(kUnevenChunk) uneven_hist(UnevenArgs* _
   if (threadIdx.x == kUnevenInvalid && h[kUnevenInvalid] > 0) atomicOr(err, kErrUnevenSkipped);
 }
 
+// Grid of size bin b's kernel from the bucket counts (transforms per size,
+// sizes 8 << i): one CTA per tile when the size holds at least 90 % of the
+// batch's bytes (or its tiles fit in one wave of resident CTAs), else a
+// persistent grid of `wave` CTAs.  At least 1.
+FFTOC_HD long long uneven_grid(const int* counts, int b, int tpb, int wave) {
+  double bytes = 0.0;
+  for (int i = 0; i < kUnevenInvalid; ++i) bytes += (double)counts[i] * (double)(8 << i);
+  const double share = bytes > 0.0 ? (double)counts[b] * (double)(8 << b) / bytes : 1.0;
+  const long long tiles = ((long long)counts[b] + tpb - 1) / tpb;
+  const long long grid = share >= 0.9 || tiles < wave ? tiles : wave;
+  return grid > 0 ? grid : 1;
+}
+
 // One CTA of 32 x kUnevenBins threads: warp b scans bin b over the chunks.
 // With `size_nodes` (launched from the graph), the size kernels' grids are
 // set from the bucket counts.
@@ -125,13 +138,7 @@ static __global__ void __launch_bounds__(32 * kUnevenBins) uneven_scan(UnevenArg
     // faster on mixed batches than one CTA per tile, whose grids then run
     // one after another, and than grids in proportion to each size's bytes).
     const int b = threadIdx.x;
-    double bytes = 0.0;
-    for (int i = 0; i < kUnevenInvalid; ++i) bytes += (double)total[i] * (double)(8 << i);
-    const double share = bytes > 0.0 ? (double)total[b] * (double)(8 << b) / bytes : 1.0;
-    const int tpb = a->tpb[b];
-    const long long tiles = ((long long)total[b] + tpb - 1) / tpb;
-    const long long grid = share >= 0.9 || tiles < a->wave[b] ? tiles : a->wave[b];
-    cudaGraphKernelNodeSetGridDim(a->nodes[b], dim3(grid > 0 ? (unsigned)grid : 1u));
+    cudaGraphKernelNodeSetGridDim(a->nodes[b], dim3((unsigned)uneven_grid(total, b, a->tpb[b], a->wave[b])));
   }
 }
 

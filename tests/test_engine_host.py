@@ -149,3 +149,22 @@ def test_exact_pass_matches_dft(exact_report):
     stay below the 2^58.5 bound the next pass relies on."""
     assert exact_report["exact_pass_err"] < 2.0 ** -46
     assert exact_report["exact_out_log2"] <= 58.5
+
+
+def test_uneven_grid_rule():
+    """The uneven graph's grid rule (uneven_grid, evaluated on the device from
+    the bucket counts), compiled as host code: one CTA per tile for a size
+    holding at least 90 % of the batch or fewer tiles than one wave, else one
+    wave of persistent CTAs, never 0."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    out_dir = os.path.join(ROOT, "tests", "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    exe = os.path.join(out_dir, "uneven_grid_check")
+    csrc = os.path.join(ROOT, "fft_onchip_gb300", "csrc")
+    subprocess.run([nvcc, "-std=c++17", "--expt-relaxed-constexpr", "-gencode", "arch=compute_103a,code=sm_103a",
+                    "-I" + csrc, "-I" + os.path.join(ROOT, "include"), "-o", exe,
+                    os.path.join(ROOT, "tests", "host", "uneven_grid_check.cu")], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.startswith("ok"), r.stdout
