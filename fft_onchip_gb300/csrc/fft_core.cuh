@@ -40,6 +40,7 @@ struct PlanT {
   static constexpr int TPB = TPB_;
   static constexpr int MINB = MINB_;  // minimum resident CTAs per SM (register budget)
   static constexpr bool PREFETCH = false;  // batched kernel: L2 prefetch one wave ahead (Prefetched<>)
+  static constexpr long long PREFETCH_MIN_BYTES = 0;  // ... for batches of at least this much input
   static constexpr bool OUTLINE_SLOW_IN = false;  // batched kernel: rare input path out of line (OutlinedSlowIn<>)
   static constexpr bool IMAD_SPLIT = false;  // fixed point: low limbs by integer multiply-add (ImadSplit<>)
   static constexpr bool OUT_HI_ZERO = false;  // fixed point: zero test on the converted word (OutHiZero<>)
@@ -226,10 +227,13 @@ template <bool B> struct Konst<EngFxT<B>> {
 };
 
 // A plan whose batched kernel also prefetches, into L2, the tile of the CTA
-// that starts one full wave (SMs x MINB CTAs) later.
-template <class PL>
+// that starts one full wave (SMs x MINB CTAs) later, for batches of at least
+// MIN_MIB MiB of input (below that the prefetch measured slower at some sizes:
+// N = 64 by 16 % at 64 MiB, N = 4096 by 1-2 % up to 256 MiB).
+template <class PL, int MIN_MIB = 0>
 struct Prefetched : PL {
   static constexpr bool PREFETCH = true;
+  static constexpr long long PREFETCH_MIN_BYTES = (long long)MIN_MIB << 20;
 };
 
 // A plan whose batched kernel converts the rare transforms that leave the

@@ -599,7 +599,7 @@ fft_fwd_kernel(const double2* __restrict__ in, double2* __restrict__ out, long l
   longlong2* sm = reinterpret_cast<longlong2*>(smem_raw);
 
   if constexpr (PL::PREFETCH) {
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && batch * (PL::N * 16) >= PL::PREFETCH_MIN_BYTES) {
       // the tile of the CTA that starts one full wave later, into L2
       unsigned nsm;
       asm("mov.u32 %0, %%nsmid;" : "=r"(nsm));
