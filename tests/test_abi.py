@@ -157,6 +157,19 @@ def test_small_cta_defaults_per_engine(fftoc_lib, n):
     assert _lib.plan_query(n, _lib.ENGINE_FX, variant=0)["uneven_variant"] == 1
 
 
+def test_n1024_fixed_point_default(fftoc_lib):
+    """At N = 1024 the fixed-point default runs one transform per 128-thread
+    CTA; the 256-thread plan of the same radices follows it and stays the plan
+    of the uneven-batch kernels.  The IEEE engine keeps its radix-16 default."""
+    q0, q1 = (_lib.plan_query(1024, _lib.ENGINE_FX, variant=v) for v in (0, 1))
+    assert q0["threads_per_block"] == 128 and q0["transforms_per_block"] == 1
+    assert q1["threads_per_block"] == 256 and q1["transforms_per_block"] == 2
+    assert (q0["radix"], q0["points_per_thread"]) == (q1["radix"], q1["points_per_thread"]) == ([8, 8, 8, 2], 8)
+    assert q0["code_flags"] == q1["code_flags"]
+    assert q0["uneven_variant"] == 1
+    assert _lib.plan_query(1024, _lib.ENGINE_F64, variant=0)["radix"] == [16, 16, 4]
+
+
 def test_onchip_plan_overrides(fftoc_lib):
     from fft_onchip_gb300 import onchip
     sizes = (128, 256, 512)
