@@ -14,8 +14,8 @@
 // Steps 1-3 read the transform count from device memory.  The size kernels
 // are device-updatable graph nodes whose grids uneven_scan sets from the
 // bucket counts: one CTA per tile (like the batched kernels) for a size that
-// has nearly the whole batch, else persistent grids of the size's resident
-// CTAs, the sizes side by side on parallel branches.  Where
+// holds at least 40 % of the batch's bytes, else persistent grids of the
+// size's resident CTAs, the sizes side by side on parallel branches.  Where
 // the runtime refuses device-updatable nodes, the graph keeps persistent
 // grids (the SM count times the resident CTAs) and the CTAs walk their
 // bucket tile by tile.
@@ -87,15 +87,16 @@ static __global__ void __launch_bounds__(kUnevenChunk) uneven_hist(UnevenArgs* _
 }
 
 // Grid of size bin b's kernel from the bucket counts (transforms per size,
-// sizes 8 << i): one CTA per tile when the size holds at least 90 % of the
+// sizes 8 << i): one CTA per tile when the size holds at least 40 % of the
 // batch's bytes (or its tiles fit in one wave of resident CTAs), else a
-// persistent grid of `wave` CTAs.  At least 1.
+// persistent grid of `wave` CTAs.  At least 1.  At most two sizes pass the
+// share test.
 FFTOC_HD long long uneven_grid(const int* counts, int b, int tpb, int wave) {
   double bytes = 0.0;
   for (int i = 0; i < kUnevenInvalid; ++i) bytes += (double)counts[i] * (double)(8 << i);
   const double share = bytes > 0.0 ? (double)counts[b] * (double)(8 << b) / bytes : 1.0;
   const long long tiles = ((long long)counts[b] + tpb - 1) / tpb;
-  const long long grid = share >= 0.9 || tiles < wave ? tiles : wave;
+  const long long grid = share >= 0.4 || tiles < wave ? tiles : wave;
   return grid > 0 ? grid : 1;
 }
 
@@ -131,12 +132,14 @@ static __global__ void __launch_bounds__(32 * kUnevenBins) uneven_scan(UnevenArg
     }
   }
   if (size_nodes && threadIdx.x < kUnevenInvalid && a->nodes[threadIdx.x] != nullptr) {
-    // A size with nearly all of the batch's bytes runs one CTA per tile
-    // (measured 9-15 % faster alone at N = 512..4096).  Sizes that share the
-    // batch keep persistent grids of their resident CTAs on the device, so
-    // that each can use the whole device as the others finish (measured
-    // faster on mixed batches than one CTA per tile, whose grids then run
-    // one after another, and than grids in proportion to each size's bytes).
+    // A size with at least 40 % of the batch's bytes runs one CTA per tile
+    // (measured 9-15 % faster alone at N = 512..4096, and 1.8 % faster on a
+    // mixed batch whose N = 4096 transforms hold 45 % of the bytes).  The
+    // other sizes keep persistent grids of their resident CTAs on the device,
+    // so that each can use the whole device as the others finish (measured
+    // faster on mixed batches than one CTA per tile for every size, whose
+    // grids then run one after another, and than grids in proportion to each
+    // size's bytes).
     const int b = threadIdx.x;
     cudaGraphKernelNodeSetGridDim(a->nodes[b], dim3((unsigned)uneven_grid(total, b, a->tpb[b], a->wave[b])));
   }

@@ -154,7 +154,7 @@ def test_exact_pass_matches_dft(exact_report):
 def test_uneven_grid_rule():
     """The uneven graph's grid rule (uneven_grid, evaluated on the device from
     the bucket counts), compiled as host code: one CTA per tile for a size
-    holding at least 90 % of the batch or fewer tiles than one wave, else one
+    holding at least 40 % of the batch's bytes or fewer tiles than one wave, else one
     wave of persistent CTAs, never 0."""
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
